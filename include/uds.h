@@ -1,0 +1,151 @@
+/* uds.h - C ABI of the GB300 splatting library (libuds.so).
+ *
+ * One entry point per operation of the reference's torch extensions
+ * (cudaExtensions.{transform,sampling,splatting,filtering,interpolation,
+ * shading}); each comment names the reference host wrapper it replaces.
+ *
+ * Conventions shared by every entry point:
+ *  - all pointers are CUDA device pointers to contiguous float32 / int32
+ *    arrays in the reference's layouts: splat arrays (1|B, N, c), pixel arrays
+ *    (B, W, H, ...) with pixel offset j + H*i for x = i, y = j;
+ *  - `stream` is a cudaStream_t (NULL = legacy default stream); work is only
+ *    enqueued, nothing synchronises with the host;
+ *  - outputs are written completely (gradient outputs are zeroed first), so
+ *    callers may pass uninitialised memory;
+ *  - scratch memory is caller-owned: query its size with the matching
+ *    *_workspace_size function and pass a device buffer of at least that many
+ *    bytes (16-byte aligned).  Nothing here calls cudaMalloc, so every call is
+ *    safe inside CUDA graph capture;
+ *  - the return value is a uds_status; uds_status_string() names it.
+ */
+#ifndef UDS_H
+#define UDS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    UDS_OK = 0,
+    UDS_ERR_ARGUMENT = 1,   /* bad size, NULL pointer, unsupported K, ... */
+    UDS_ERR_WORKSPACE = 2,  /* workspace smaller than the query returned */
+    UDS_ERR_LAUNCH = 3,     /* a kernel launch failed (cudaGetLastError) */
+    UDS_ERR_CUDA = 4        /* another CUDA runtime error */
+} uds_status;
+
+const char* uds_status_string(int status);
+/* Last CUDA error text seen by a failing call on this host thread. */
+const char* uds_last_error(void);
+int uds_version(void);
+
+/* Per-view record written by uds_sample (32 bytes). */
+typedef struct {
+    float h;          /* isotropic FGT bandwidth in pixels (samplingCuda.cu:233-248) */
+    float radius;     /* cull radius (samplingCuda.cu:251-252) */
+    int32_t n_visible;/* splats that survived culling = tree leaves */
+    int32_t n_coefs;  /* Hermite coefficients stored for internal nodes */
+    int32_t demoted;  /* nodes whose expansion did not fit the coefficient pool */
+    int32_t overflow; /* pixels whose descent exceeded the 64-entry trace */
+    int32_t reserved[2];
+} uds_view_stats;
+
+/* Sampling parameters (sampling.cpp:48-94 plus the uniforms interface). */
+typedef struct {
+    int32_t B, N, W, H, K;   /* views, splats per view, image size, samples per pixel */
+    float focal;             /* focal length in pixels */
+    float smoothing;         /* added to the screen-space covariance */
+    float precision;         /* FGT truncation precision */
+    int32_t max_degree;      /* cap of the adaptive Hermite degree (<= 16) */
+    int32_t std_batch;       /* leading dim of stdDevs: 1 or B */
+    int64_t coef_pool;       /* coefficient pool size in floats (<=0: default) */
+    uint64_t seed;           /* Philox key when `uniforms` is NULL */
+} uds_sample_params;
+
+/* ---- transform (transform.cpp:33-86: affineForward/Backward,
+ *      linearForward/Backward).  M (B,4,4), v (vB,N,3) -> out (B,N,3). ---- */
+int uds_transform_forward(int affine, int B, const float* M, int vB, int N, const float* v,
+                          float* out, void* stream);
+/* gM (B,4,4) and gv (vB,N,3) are overwritten. */
+int uds_transform_backward(int affine, int B, const float* grad, const float* M, int vB, int N,
+                           const float* v, float* gM, float* gv, void* stream);
+
+/* ---- sampling.sample (sampling.cpp:48-94): points, normals (B,N,3)
+ *      camera space, stdDevs (std_batch,N,2) -> indices (B,W,H,K) int32,
+ *      -1 where no sample.  uniforms: optional (B,W,H,R,K) float32 in (0,1],
+ *      R = ceil(sqrt(K)); NULL draws Philox4x32-10 uniforms from seed.
+ *      h_override: optional device float[B]; entries > 0 replace the
+ *      computed bandwidth.  stats: device uds_view_stats[B] (may be NULL). ---- */
+size_t uds_sample_workspace_size(const uds_sample_params* prm);
+int uds_sample(const uds_sample_params* prm, const float* points, const float* normals,
+               const float* std_devs, const float* uniforms, const float* h_override,
+               int32_t* indices, uds_view_stats* stats, void* workspace, size_t workspace_bytes,
+               void* stream);
+
+/* Debug view of one tree (for tests): builds view `view` and copies the
+ * first n_visible entries of each array (host-sized by the caller from
+ * stats).  Any output pointer may be NULL.  Arrays: keys/ids (n), node arrays
+ * (2n-1): left, right, parent, count, degree; centre (2n-1,2); box (2n-1,4). */
+int uds_tree_build(const uds_sample_params* prm, int view, const float* points,
+                   const float* normals, const float* std_devs, const float* h_override,
+                   uds_view_stats* stats, uint32_t* keys, int32_t* ids, int32_t* left,
+                   int32_t* right, int32_t* parent, int32_t* count, int32_t* degree,
+                   float* centre, float* box, void* workspace, size_t workspace_bytes,
+                   void* stream);
+/* FGT node masses (getWeight) of an already built tree (same workspace,
+ * after uds_tree_build): m queries (node id, x, y) -> out[m]. */
+int uds_fgt_eval(const uds_sample_params* prm, int m, const int32_t* nodes, const float* query_xy,
+                 float* out, const void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- splatting.forward / backward (splatting.cpp:43-129).  points,
+ *      normals (B,N,3) camera space; std_devs (std_batch,N,2); weights and
+ *      grad (B,W,H,K).  Workspace: per-splat Gaussian constants and gradient
+ *      statistics, uds_splat_workspace_size(B, N) bytes. ---- */
+size_t uds_splat_workspace_size(int B, int N);
+int uds_splat_forward(int B, int W, int H, int K, float focal, const int32_t* indices,
+                      const float* points, const float* normals, int std_batch, int N,
+                      const float* std_devs, float smoothing, float* weights, void* workspace,
+                      size_t workspace_bytes, void* stream);
+int uds_splat_backward(int B, int W, int H, int K, float focal, const float* grad,
+                       const int32_t* indices, const float* points, const float* normals,
+                       int std_batch, int N, const float* std_devs, float smoothing,
+                       float* grad_points, float* grad_normals, float* grad_std_devs,
+                       void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- filtering.forward / backward (zSorting.cpp:24-43); points/normals
+ *      (pB,N,3), pB = 1 or B. ---- */
+int uds_filter_forward(int B, int W, int H, int K, const int32_t* indices, const float* weights,
+                       float focal, int pB, int N, const float* points, const float* normals,
+                       float* out, void* stream);
+int uds_filter_backward(int B, int W, int H, int K, const int32_t* indices, const float* weights,
+                        const float* grad, float focal, int pB, int N, const float* points,
+                        const float* normals, float* grad_weights, void* stream);
+
+/* ---- interpolation.forward / backward (interpolation.cpp:31-95);
+ *      attribute (aB,N,C). ---- */
+int uds_interp_forward(int B, int W, int H, int K, const int32_t* indices, const float* weights,
+                       int aB, int N, int C, const float* attribute, float* out, void* stream);
+int uds_interp_backward(int B, int W, int H, int K, const float* grad, const int32_t* indices,
+                        const float* weights, int aB, int N, int C, const float* attribute,
+                        float* grad_weights, float* grad_attribute, void* stream);
+
+/* ---- shading.forward / backward / forwardSh / backwardSh
+ *      (shading.cpp:51-199).  Pixels P = W*H per view. ---- */
+int uds_shade_forward(int B, int P, int L, const float* dirs, const float* intensities, int IB,
+                      const float* normals, const float* diffuse, float* out, void* stream);
+int uds_shade_backward(int B, int P, int L, const float* grad, const float* dirs,
+                       const float* intensities, int IB, const float* normals,
+                       const float* diffuse, float* grad_dirs, float* grad_intensities,
+                       float* grad_normals, float* grad_diffuse, void* stream);
+int uds_shade_sh_forward(int B, int P, const float* coeffs, int cB, const float* normals,
+                         const float* diffuse, float* out, void* stream);
+int uds_shade_sh_backward(int B, int P, const float* grad, const float* coeffs, int cB,
+                          const float* normals, const float* diffuse, float* grad_coeffs,
+                          float* grad_normals, float* grad_diffuse, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,255 @@
+// splatting.forward / splatting.backward (splatting.cpp:43-129,
+// splattingCuda.cu:18-233) restructured for the GPU:
+//   forward : per-splat Gaussian constants once (the part of the reference's
+//             per-sample work that does not depend on the pixel), then one
+//             thread per pixel evaluates its K samples;
+//   backward: per sample only the sufficient statistics of the gradient
+//             (sum g*G, sum g*G*d, sum g*G*d d^T, d = pixel - screen point)
+//             are scattered, then one thread per splat applies the chain
+//             rule through covariance, Jacobian, tangent plane and
+//             projection once.  The reference instead runs the full chain
+//             (ewaSplattingGrad.cuh:163-206) per sample and scatters 8 floats.
+#include "uds_ewa.cuh"
+
+namespace uds {
+
+__global__ void k_ewa_consts(int B, int N, float W, float H, float f,
+                             const float* __restrict__ pts, const float* __restrict__ nrm,
+                             const float* __restrict__ sd, int sdB, float sm,
+                             float4* __restrict__ consts) {
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    int b = blockIdx.y;
+    if (x >= N) return;
+    size_t o = (size_t)x + (size_t)N * b;
+    float p[3] = {pts[3 * o], pts[3 * o + 1], pts[3 * o + 2]};
+    float n[3] = {nrm[3 * o], nrm[3 * o + 1], nrm[3 * o + 2]};
+    size_t so = sdB > 1 ? o : (size_t)x;
+    float s[2] = {sd[2 * so], sd[2 * so + 1]};
+    EwaFrame F;
+    ewa_frame(W, H, f, p, n, s, sm, F);
+    float4 a, c;
+    ewa_gauss_consts(F, a, c);
+    consts[2 * o] = a;
+    consts[2 * o + 1] = c;
+}
+
+// One thread per pixel (x = i, y = j), K samples.
+__global__ void k_ewa_forward(int B, int W, int H, int K, const int* __restrict__ idx,
+                              const float4* __restrict__ consts, int N, float* __restrict__ w) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    int i = blockIdx.y;
+    int b = blockIdx.z;
+    if (j >= H) return;
+    size_t pix = (size_t)j + (size_t)H * ((size_t)i + (size_t)W * b);
+    float px = (float)i, py = (float)j;
+    for (int s = 0; s < K; ++s) {
+        size_t off = (size_t)s + (size_t)K * pix;
+        int id = idx[off];
+        float out = 0.0f;
+        if (id >= 0) {
+            size_t o = (size_t)id + (size_t)N * b;
+            float4 a = consts[2 * o], c = consts[2 * o + 1];
+            out = fminf(ewa_gauss(a, c, px, py), 1.0f);
+        }
+        w[off] = out;
+    }
+}
+
+// Sufficient statistics of the EWA gradient, gated on the unclamped weight
+// <= 1 like gradEwaKernel (splattingCuda.cu:173).
+__global__ void k_ewa_stats(int B, int W, int H, int K, const float* __restrict__ grad,
+                            const int* __restrict__ idx, const float4* __restrict__ consts, int N,
+                            float4* __restrict__ stats) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    int i = blockIdx.y;
+    int b = blockIdx.z;
+    if (j >= H) return;
+    size_t pix = (size_t)j + (size_t)H * ((size_t)i + (size_t)W * b);
+    float px = (float)i, py = (float)j;
+    for (int s = 0; s < K; ++s) {
+        size_t off = (size_t)s + (size_t)K * pix;
+        int id = idx[off];
+        if (id < 0) continue;
+        size_t o = (size_t)id + (size_t)N * b;
+        float4 a = consts[2 * o], c = consts[2 * o + 1];
+        float dx, dy;
+        float G = ewa_gauss(a, c, px, py, &dx, &dy);
+        if (!(G <= 1.0f)) continue;
+        float g = grad[off] * G;
+        if (g == 0.0f) continue;
+        atomicAdd(&stats[2 * o], make_float4(g, g * dx, g * dy, g * dx * dx));
+        atomicAdd(reinterpret_cast<float2*>(&stats[2 * o + 1]), make_float2(g * dx * dy, g * dy * dy));
+    }
+}
+
+__device__ __forceinline__ void cross3(const float* a, const float* b, float* c) {
+    c[0] = a[1] * b[2] - a[2] * b[1];
+    c[1] = a[2] * b[0] - a[0] * b[2];
+    c[2] = a[0] * b[1] - a[1] * b[0];
+}
+__device__ __forceinline__ float dot3c(const float* a, const float* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+// Reverse-mode chain of the EWA weight for one splat from its statistics.
+__global__ void k_ewa_chain(int B, int N, float W, float H, float f, const float* __restrict__ pts,
+                            const float* __restrict__ nrm, const float* __restrict__ sd, int sdB,
+                            float sm, const float4* __restrict__ stats, float* __restrict__ gp_out,
+                            float* __restrict__ gn_out, float* __restrict__ gs_out) {
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    int b = blockIdx.y;
+    if (x >= N) return;
+    size_t o = (size_t)x + (size_t)N * b;
+    float4 st0 = stats[2 * o], st1 = stats[2 * o + 1];
+    float S0 = st0.x, S1x = st0.y, S1y = st0.z, S2xx = st0.w, S2xy = st1.x, S2yy = st1.y;
+    size_t so = sdB > 1 ? o : (size_t)x;
+    if (S0 == 0.0f && S1x == 0.0f && S1y == 0.0f && S2xx == 0.0f && S2xy == 0.0f && S2yy == 0.0f) {
+        gp_out[3 * o] = 0.0f; gp_out[3 * o + 1] = 0.0f; gp_out[3 * o + 2] = 0.0f;
+        gn_out[3 * o] = 0.0f; gn_out[3 * o + 1] = 0.0f; gn_out[3 * o + 2] = 0.0f;
+        if (sdB > 1) { gs_out[2 * so] = 0.0f; gs_out[2 * so + 1] = 0.0f; }
+        return;
+    }
+    float p[3] = {pts[3 * o], pts[3 * o + 1], pts[3 * o + 2]};
+    float n[3] = {nrm[3 * o], nrm[3 * o + 1], nrm[3 * o + 2]};
+    float sdv[2] = {sd[2 * so], sd[2 * so + 1]};
+    // forward quantities (same sequence as the frame)
+    float sp[2];
+    screen_point(W, H, f, p, sp);
+    float y0[2] = {(float)dadd((double)sp[0], 1.0), sp[1]};
+    float y1[2] = {sp[0], (float)dadd((double)sp[1], 1.0)};
+    float x0[3], x1[3], t0[3], t1[3];
+    back_project(W, H, f, y0, x0);
+    back_project(W, H, f, y1, x1);
+    float c = dot3(p, n);
+    float D0 = dot3(x0, n), D1 = dot3(x1, n);
+    float k0 = fdiv(c, D0), k1 = fdiv(c, D1);
+    tangent(x0, p, n, t0);
+    tangent(x1, p, n, t1);
+    float al = fsqrt(dot3(t0, t0));
+    float invNorm = (float)ddiv(1.0, (double)al);
+    float u0[3] = {t0[0] * invNorm, t0[1] * invNorm, t0[2] * invNorm};
+    float u1[3];
+    cross3(u0, n, u1);
+    float be = dot3c(t1, u0), ga = dot3c(t1, u1);
+    float J00 = 1.0f / al, J01 = -be / (al * ga), J11 = 1.0f / ga;
+    float Sg0 = sdv[0] * sdv[0], Sg1 = sdv[1] * sdv[1];
+    float V00 = J00 * J00 * Sg0 + J01 * J01 * Sg1 + sm;
+    float V01 = J01 * J11 * Sg1;
+    float V11 = J11 * J11 * Sg1 + sm;
+    float vdet = V00 * V11 - V01 * V01;
+    float I00 = V11 / vdet, I01 = -V01 / vdet, I11 = V00 / vdet;
+    // moments of q = V^-1 d
+    float M1x = I00 * S1x + I01 * S1y, M1y = I01 * S1x + I11 * S1y;
+    float A00 = I00 * S2xx + I01 * S2xy, A01 = I00 * S2xy + I01 * S2yy;
+    float A10 = I01 * S2xx + I11 * S2xy, A11 = I01 * S2xy + I11 * S2yy;
+    float Q00 = A00 * I00 + A01 * I01, Q01 = A00 * I01 + A01 * I11, Q11 = A10 * I01 + A11 * I11;
+    float gV00 = 0.5f * (Q00 - S0 * I00), gV01 = 0.5f * (Q01 - S0 * I01), gV11 = 0.5f * (Q11 - S0 * I11);
+    float gJ00 = 2.0f * (gV00 * J00 * Sg0);
+    float gJ01 = 2.0f * (gV00 * J01 * Sg1 + gV01 * J11 * Sg1);
+    float gJ11 = 2.0f * (gV01 * J01 * Sg1 + gV11 * J11 * Sg1);
+    float gsd0 = 2.0f * sdv[0] * (J00 * J00 * gV00);
+    float gsd1 = 2.0f * sdv[1] * (J01 * J01 * gV00 + 2.0f * J01 * J11 * gV01 + J11 * J11 * gV11);
+    float gal = -gJ00 / (al * al) + gJ01 * be / (al * al * ga) - S0 / al;
+    float gbe = -gJ01 / (al * ga);
+    float gga = gJ01 * be / (al * ga * ga) - gJ11 / (ga * ga) - S0 / ga;
+    float nxt1[3], t1xu0[3], gt1[3], gu0[3], gnv[3];
+    cross3(n, t1, nxt1);
+    cross3(t1, u0, t1xu0);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        gt1[i] = gbe * u0[i] + gga * u1[i];
+        gu0[i] = gbe * t1[i] + gga * nxt1[i];
+        gnv[i] = gga * t1xu0[i];
+    }
+    float gdu = dot3c(gu0, u0), gt0[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) gt0[i] = (gu0[i] - gdu * u0[i]) / al + gal * u0[i];
+    float gpv[3] = {-gt0[0] - gt1[0], -gt0[1] - gt1[1], -gt0[2] - gt1[2]};
+    float gk0 = dot3c(gt0, x0), gk1 = dot3c(gt1, x1);
+    float gc = gk0 / D0 + gk1 / D1;
+    float gD0 = -gk0 * c / (D0 * D0), gD1 = -gk1 * c / (D1 * D1);
+    float gx00 = k0 * gt0[0] + gD0 * n[0], gx01 = k0 * gt0[1] + gD0 * n[1];
+    float gx10 = k1 * gt1[0] + gD1 * n[0], gx11 = k1 * gt1[1] + gD1 * n[1];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        gnv[i] += gD0 * x0[i] + gD1 * x1[i] + gc * p[i];
+        gpv[i] += gc * n[i];
+    }
+    float gS0 = M1x - (gx00 + gx10) / f;
+    float gS1 = M1y + (gx01 + gx11) / f;
+    float iz = 1.0f / p[2];
+    gpv[0] += gS0 * (-f * iz);
+    gpv[1] += gS1 * (f * iz);
+    gpv[2] += (gS0 * p[0] - gS1 * p[1]) * f * iz * iz;
+    gp_out[3 * o] = gpv[0]; gp_out[3 * o + 1] = gpv[1]; gp_out[3 * o + 2] = gpv[2];
+    gn_out[3 * o] = gnv[0]; gn_out[3 * o + 1] = gnv[1]; gn_out[3 * o + 2] = gnv[2];
+    if (sdB > 1) {
+        gs_out[2 * so] = gsd0;
+        gs_out[2 * so + 1] = gsd1;
+    } else {
+        atomicAdd(&gs_out[2 * so], gsd0);
+        atomicAdd(&gs_out[2 * so + 1], gsd1);
+    }
+}
+
+}  // namespace uds
+
+using namespace uds;
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+extern "C" size_t uds_splat_workspace_size(int B, int N) {
+    return align256(sizeof(float4) * 2 * (size_t)B * N) * 2;
+}
+
+static int check_splat_args(int B, int W, int H, int K, int std_batch, int N) {
+    if (B <= 0 || W <= 0 || H <= 0 || K <= 0 || N < 0) return UDS_ERR_ARGUMENT;
+    if (std_batch != 1 && std_batch != B) return UDS_ERR_ARGUMENT;
+    return UDS_OK;
+}
+
+extern "C" int uds_splat_forward(int B, int W, int H, int K, float focal, const int32_t* indices,
+                                 const float* points, const float* normals, int std_batch, int N,
+                                 const float* std_devs, float smoothing, float* weights,
+                                 void* workspace, size_t workspace_bytes, void* stream) {
+    int st = check_splat_args(B, W, H, K, std_batch, N);
+    if (st) return st;
+    if (!indices || !weights) return UDS_ERR_ARGUMENT;
+    if (workspace_bytes < uds_splat_workspace_size(B, N) || (N > 0 && !workspace)) return UDS_ERR_WORKSPACE;
+    cudaStream_t s = as_stream(stream);
+    float4* consts = reinterpret_cast<float4*>(workspace);
+    if (N > 0) {
+        k_ewa_consts<<<dim3(cdiv(N, 128), B), 128, 0, s>>>(B, N, (float)W, (float)H, focal, points, normals,
+                                                          std_devs, std_batch, smoothing, consts);
+        if ((st = launch_status())) return st;
+    }
+    k_ewa_forward<<<dim3(cdiv(H, 64), W, B), 64, 0, s>>>(B, W, H, K, indices, consts, N, weights);
+    return launch_status();
+}
+
+extern "C" int uds_splat_backward(int B, int W, int H, int K, float focal, const float* grad,
+                                  const int32_t* indices, const float* points, const float* normals,
+                                  int std_batch, int N, const float* std_devs, float smoothing,
+                                  float* grad_points, float* grad_normals, float* grad_std_devs,
+                                  void* workspace, size_t workspace_bytes, void* stream) {
+    int st = check_splat_args(B, W, H, K, std_batch, N);
+    if (st) return st;
+    if (!grad || !indices) return UDS_ERR_ARGUMENT;
+    if (workspace_bytes < uds_splat_workspace_size(B, N) || (N > 0 && !workspace)) return UDS_ERR_WORKSPACE;
+    if (N == 0) return UDS_OK;
+    cudaStream_t s = as_stream(stream);
+    float4* consts = reinterpret_cast<float4*>(workspace);
+    float4* stats = reinterpret_cast<float4*>(reinterpret_cast<char*>(workspace) +
+                                              align256(sizeof(float4) * 2 * (size_t)B * N));
+    cudaError_t e = cudaMemsetAsync(stats, 0, sizeof(float4) * 2 * (size_t)B * N, s);
+    if (e == cudaSuccess && std_batch == 1)
+        e = cudaMemsetAsync(grad_std_devs, 0, sizeof(float) * 2 * (size_t)N, s);
+    if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
+    k_ewa_consts<<<dim3(cdiv(N, 128), B), 128, 0, s>>>(B, N, (float)W, (float)H, focal, points, normals,
+                                                      std_devs, std_batch, smoothing, consts);
+    if ((st = launch_status())) return st;
+    k_ewa_stats<<<dim3(cdiv(H, 64), W, B), 64, 0, s>>>(B, W, H, K, grad, indices, consts, N, stats);
+    if ((st = launch_status())) return st;
+    k_ewa_chain<<<dim3(cdiv(N, 128), B), 128, 0, s>>>(B, N, (float)W, (float)H, focal, points, normals,
+                                                     std_devs, std_batch, smoothing, stats, grad_points,
+                                                     grad_normals, grad_std_devs);
+    return launch_status();
+}

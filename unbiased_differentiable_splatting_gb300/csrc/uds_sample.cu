@@ -1,0 +1,937 @@
+// sampling.sample (sampling.cpp:48-94, samplingCuda.cu:197-321) on one GPU:
+// per view, the FMM tree over the projected splat centres and the per-pixel
+// sequential-Poisson descent that draws K splat indices.
+//
+// Pipeline per view (all on the caller's stream, no host synchronisation;
+// view-dependent sizes are read on the device):
+//   1 k_bandwidth / k_view_setup  isotropic bandwidth h (mean over splats,
+//                                 fixed point) and the cull radius
+//   2 k_cull_morton               screen point, visibility, 30-bit Morton key;
+//                                 culled splats get a key above every
+//                                 visible one so a single sort compacts
+//   3 radix sort                  LSD, 4 x 8-bit passes, stable, hand-written
+//   4 k_leaves / k_karras         Karras (2012) radix tree over 64-bit keys
+//                                 (key << 32 | rank)
+//   5 k_bottomup                  atomic fan-in: boxes, count-weighted
+//                                 centres, adaptive Hermite degree,
+//                                 truncation radius
+//   6 node sizes -> scan -> k_assign   coefficient offsets in a fixed pool
+//   7 k_p2m                       Hermite moments, one warp per node, each
+//                                 coefficient summed over the node's leaves in
+//                                 Morton order (deterministic, no atomics)
+//   8 k_sample                    per pixel: ceil(sqrt(K)) rounds of greedy
+//                                 capacity descent + order sampling on u/p
+//
+// Every float operation on this path is spelled with an exact-rounding
+// intrinsic (or is an IEEE-exact library op: sqrt, division, fma), so the
+// Morton keys, the tree, the FGT masses and the sampled indices equal the CPU
+// oracle's bit for bit given the same inputs and uniforms.
+#include "uds_ewa.cuh"
+
+namespace uds {
+
+constexpr unsigned kCulledKey = 0x40000000u;  // above every 30-bit Morton key
+constexpr int kSortThreads = 256, kSortItems = 8, kSortTile = kSortThreads * kSortItems;
+constexpr int kScanThreads = 256, kScanItems = 4, kScanTile = kScanThreads * kScanItems;
+
+struct ViewState {            // per-view device scalars (lives in the workspace)
+    unsigned long long hsum;  // fixed-point sum of per-splat bandwidths (2^-32 units)
+    unsigned long long hcount;
+    float h, radius, lo_x, hi_x, lo_y, hi_y, sq;  // sq = sqrt(2 h^2)
+    int n;                    // visible splats
+    unsigned coef_used;
+    int pad[5];
+};
+
+// ----------------------------------------------------------- workspace
+struct Ws {
+    ViewState* vs;
+    uds_view_stats* stats;
+    uint32_t *keysA, *idsA, *keysB, *idsB;
+    uint32_t* hist;
+    uint32_t* scanTmp;
+    uint32_t* sizes;
+    uint32_t* offsets;
+    unsigned* fanin;
+    float2* leaf_xy;
+    int* leaf_id;
+    int4* lnk;
+    int* par;
+    float4* box;
+    float4* cen;
+    float* coef;
+    size_t coef_cap;
+    size_t bytes;
+};
+
+static size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+static int64_t default_pool(int64_t N) { return N * 64 > (1 << 20) ? N * 64 : (1 << 20); }
+
+static Ws layout(const uds_sample_params* p, char* base) {
+    Ws w{};
+    size_t N = (size_t)(p->N > 0 ? p->N : 1);
+    size_t M = 2 * N;
+    size_t nb = cdiv(N, kSortTile);
+    size_t sb = cdiv(N, kScanTile);
+    int64_t pool = p->coef_pool > 0 ? p->coef_pool : default_pool((int64_t)N);
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off += a256(bytes); return base ? base + o : nullptr; };
+    w.vs = (ViewState*)take(sizeof(ViewState));
+    w.stats = (uds_view_stats*)take(sizeof(uds_view_stats) * (size_t)(p->B > 0 ? p->B : 1));
+    w.keysA = (uint32_t*)take(4 * N);
+    w.idsA = (uint32_t*)take(4 * N);
+    w.keysB = (uint32_t*)take(4 * N);
+    w.idsB = (uint32_t*)take(4 * N);
+    w.hist = (uint32_t*)take(4 * 256 * nb);
+    w.scanTmp = (uint32_t*)take(4 * (sb + 1));
+    w.sizes = (uint32_t*)take(4 * N);
+    w.offsets = (uint32_t*)take(4 * N);
+    w.fanin = (unsigned*)take(4 * N);
+    w.leaf_xy = (float2*)take(8 * N);
+    w.leaf_id = (int*)take(4 * N);
+    w.lnk = (int4*)take(16 * M);
+    w.par = (int*)take(4 * M);
+    w.box = (float4*)take(16 * M);
+    w.cen = (float4*)take(16 * M);
+    w.coef = (float*)take(4 * (size_t)pool);
+    w.coef_cap = (size_t)pool;
+    w.bytes = off;
+    return w;
+}
+
+// --------------------------------------------------------- 1 bandwidth
+// IsotropicEigenFunctor (samplingCuda.cu:133-162) with the same float /
+// double promotions.
+__device__ __forceinline__ float splat_bandwidth(float W, float H, float f, const float* p,
+                                                 const float* n, const float* sd, float sm) {
+    EwaFrame F;
+    ewa_frame(W, H, f, p, n, sd, sm, F);
+    const float* V = F.V;
+    float det = fsub(fmul(V[0], V[3]), fmul(V[1], V[2]));
+    float inv = (float)ddiv(1.0, (double)det);
+    float i0 = fmul(V[3], inv), i1 = fmul(-V[1], inv), i2 = fmul(-V[2], inv), i3 = fmul(V[0], inv);
+    float tr = fadd(i0, i3);
+    float idet = fsub(fmul(i0, i3), fmul(i1, i2));
+    float root = fsqrt((float)dsub(dmul(0.25, (double)fmul(tr, tr)), (double)idet));
+    float l1 = (float)dadd(dmul(0.5, (double)tr), (double)root);
+    float l2 = (float)dsub(dmul(0.5, (double)tr), (double)root);
+    float lk = fminf(l1, l2);
+    return (float)fmin(1.0, ddiv(1.0, (double)fsqrt(lk)));
+}
+
+__global__ void k_bandwidth(int N, float W, float H, float f, const float* __restrict__ pts,
+                            const float* __restrict__ nrm, const float* __restrict__ sd, float sm,
+                            ViewState* vs) {
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long s = 0, c = 0;
+    if (x < N) {
+        float p[3] = {pts[3 * (size_t)x], pts[3 * (size_t)x + 1], pts[3 * (size_t)x + 2]};
+        float n[3] = {nrm[3 * (size_t)x], nrm[3 * (size_t)x + 1], nrm[3 * (size_t)x + 2]};
+        float d[2] = {sd[2 * (size_t)x], sd[2 * (size_t)x + 1]};
+        float hk = splat_bandwidth(W, H, f, p, n, d, sm);
+        if (isfinite(hk)) {
+            s = (unsigned long long)__double2ll_rn(dmul((double)hk, 4294967296.0));
+            c = 1;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+        c += __shfl_xor_sync(0xffffffffu, c, o);
+    }
+    if ((threadIdx.x & 31) == 0 && c) {
+        atomicAdd(&vs->hsum, s);
+        atomicAdd(&vs->hcount, c);
+    }
+}
+
+// h (or its override), the cull radius and bounds (samplingCuda.cu:244-258)
+__global__ void k_view_setup(const float* h_override, int view, float W, float H, float precision,
+                             ViewState* vs, uds_view_stats* stats) {
+    float h;
+    if (h_override && h_override[view] > 0.0f) h = h_override[view];
+    else if (vs->hcount == 0) h = __int_as_float(0x7fc00000);
+    else h = (float)ddiv(ddiv(__ull2double_rn(vs->hsum), 4294967296.0), __ull2double_rn(vs->hcount));
+    float norm = (float)dmul(2.0 * kPi, (double)fsqrt(h));
+    double a = -(double)det_logf(precision);
+    double b = (double)det_logf(norm);
+    float r = (float)dmul(dmul(1.4142135623730951, (double)h), __dsqrt_rn(dsub(a, b)));
+    vs->h = h;
+    vs->radius = r;
+    vs->lo_x = -r;
+    vs->hi_x = fadd(W, r);
+    vs->lo_y = -r;
+    vs->hi_y = fadd(H, r);
+    vs->sq = fsqrt(fmul(fmul(2.0f, h), h));
+    vs->n = 0;
+    vs->coef_used = 0;
+    stats[view].h = h;
+    stats[view].radius = r;
+    stats[view].n_visible = 0;
+    stats[view].n_coefs = 0;
+    stats[view].demoted = 0;
+    stats[view].overflow = 0;
+}
+
+// ------------------------------------------------------- 2 cull + Morton
+__device__ __forceinline__ unsigned expand_bits(unsigned v) {
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
+__device__ __forceinline__ unsigned morton_coord(float s, float lo, float hi) {
+    float src = fdiv(fsub(s, lo), fsub(hi, lo));
+    float c = fminf(fmaxf(fmul(src, 1024.0f), 0.0f), 1023.0f);
+    return (unsigned)c;
+}
+
+__global__ void k_cull_morton(int N, float W, float H, float f, const float* __restrict__ pts,
+                              ViewState* vs, uint32_t* __restrict__ keys, uint32_t* __restrict__ ids) {
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    bool vis = false;
+    if (x < N) {
+        float p[3] = {pts[3 * (size_t)x], pts[3 * (size_t)x + 1], pts[3 * (size_t)x + 2]};
+        float s[2];
+        screen_point(W, H, f, p, s);
+        float lx = vs->lo_x, hx = vs->hi_x, ly = vs->lo_y, hy = vs->hi_y;
+        vis = (p[2] <= 0.0f) && (lx <= s[0]) && (hx >= s[0]) && (ly <= s[1]) && (hy >= s[1]);
+        unsigned key = kCulledKey;
+        if (vis) key = 2u * expand_bits(morton_coord(s[0], lx, hx)) + expand_bits(morton_coord(s[1], ly, hy));
+        keys[x] = key;
+        ids[x] = (uint32_t)x;
+    }
+    unsigned ball = __ballot_sync(0xffffffffu, vis);
+    if ((threadIdx.x & 31) == 0 && ball) atomicAdd(&vs->n, __popc(ball));
+}
+
+// ---------------------------------------------------------- 3 radix sort
+// Tile of 2048 items per block: warp w owns items [w*256, w*256+256) of the
+// tile, lane l holds item w*256 + r*32 + l in round r, so (round, lane) order
+// is item order and per-warp running counts give a stable rank.
+__global__ void k_radix_hist(int N, const uint32_t* __restrict__ keys, int shift,
+                             uint32_t* __restrict__ hist) {
+    __shared__ unsigned cnt[256];
+    for (int d = threadIdx.x; d < 256; d += blockDim.x) cnt[d] = 0;
+    __syncthreads();
+    size_t base = (size_t)blockIdx.x * kSortTile;
+    for (int r = 0; r < kSortItems; ++r) {
+        size_t i = base + (size_t)r * kSortThreads + threadIdx.x;
+        if (i < (size_t)N) atomicAdd(&cnt[(keys[i] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < 256; d += blockDim.x) hist[(size_t)d * gridDim.x + blockIdx.x] = cnt[d];
+}
+
+// Exclusive scan of hist (digit-major, 256 * nb entries) in one block.
+__global__ void k_radix_scan(uint32_t* hist, int total) {
+    __shared__ uint32_t part[1024];
+    int t = threadIdx.x;
+    int per = (total + blockDim.x - 1) / blockDim.x;
+    int lo = t * per, hi = min(total, lo + per);
+    uint32_t s = 0;
+    for (int i = lo; i < hi; ++i) s += hist[i];
+    part[t] = s;
+    __syncthreads();
+    for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+        uint32_t v = t >= o ? part[t - o] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    uint32_t run = t > 0 ? part[t - 1] : 0;
+    for (int i = lo; i < hi; ++i) {
+        uint32_t v = hist[i];
+        hist[i] = run;
+        run += v;
+    }
+}
+
+__global__ void k_radix_scatter(int N, const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+                                uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, int shift,
+                                const uint32_t* __restrict__ hist) {
+    __shared__ unsigned wcnt[kSortThreads / 32][256];
+    __shared__ unsigned goff[256];
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int d = lane; d < 256; d += 32) wcnt[warp][d] = 0;
+    for (int d = threadIdx.x; d < 256; d += blockDim.x) goff[d] = hist[(size_t)d * gridDim.x + blockIdx.x];
+    __syncwarp();
+    size_t base = (size_t)blockIdx.x * kSortTile + (size_t)warp * 256;
+    uint32_t key[kSortItems], val[kSortItems];
+    unsigned rank[kSortItems];
+    unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int r = 0; r < kSortItems; ++r) {
+        size_t i = base + (size_t)r * 32 + lane;
+        bool ok = i < (size_t)N;
+        key[r] = ok ? kin[i] : 0xFFFFFFFFu;
+        val[r] = ok ? vin[i] : 0u;
+        unsigned dig = ok ? ((key[r] >> shift) & 255u) : 256u;
+        unsigned peers = __match_any_sync(0xffffffffu, dig);
+        unsigned before = 0;
+        if (ok) before = wcnt[warp][dig];
+        rank[r] = before + __popc(peers & lt);
+        __syncwarp();
+        if (ok && (peers & lt) == 0) wcnt[warp][dig] = before + __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    if (threadIdx.x < 256) {
+        unsigned run = 0;
+        for (int w = 0; w < kSortThreads / 32; ++w) {
+            unsigned c = wcnt[w][threadIdx.x];
+            wcnt[w][threadIdx.x] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kSortItems; ++r) {
+        size_t i = base + (size_t)r * 32 + lane;
+        if (i < (size_t)N) {
+            unsigned dig = (key[r] >> shift) & 255u;
+            unsigned pos = goff[dig] + wcnt[warp][dig] + rank[r];
+            kout[pos] = key[r];
+            vout[pos] = val[r];
+        }
+    }
+}
+
+// ------------------------------------------------ generic exclusive scan
+__global__ void k_scan_reduce(const uint32_t* __restrict__ in, const ViewState* vs, int minus,
+                              uint32_t* __restrict__ part) {
+    __shared__ uint32_t red[kScanThreads / 32];
+    int M = vs->n - minus;
+    size_t base = (size_t)blockIdx.x * kScanTile;
+    uint32_t s = 0;
+    for (int r = 0; r < kScanItems; ++r) {
+        size_t i = base + (size_t)r * kScanThreads + threadIdx.x;
+        if ((long long)i < M) s += in[i];
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (int w = 0; w < kScanThreads / 32; ++w) t += red[w];
+        part[blockIdx.x] = t;
+    }
+}
+
+__global__ void k_scan_top(uint32_t* part, int nb) {
+    __shared__ uint32_t buf[1024];
+    int t = threadIdx.x;
+    int per = (nb + blockDim.x - 1) / blockDim.x;
+    int lo = t * per, hi = min(nb, lo + per);
+    uint32_t s = 0;
+    for (int i = lo; i < hi; ++i) s += part[i];
+    buf[t] = s;
+    __syncthreads();
+    for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+        uint32_t v = t >= o ? buf[t - o] : 0;
+        __syncthreads();
+        buf[t] += v;
+        __syncthreads();
+    }
+    uint32_t run = t > 0 ? buf[t - 1] : 0;
+    for (int i = lo; i < hi; ++i) {
+        uint32_t v = part[i];
+        part[i] = run;
+        run += v;
+    }
+    if (t == blockDim.x - 1) part[nb] = buf[t];  // total
+}
+
+__global__ void k_scan_down(const uint32_t* __restrict__ in, const ViewState* vs, int minus,
+                            const uint32_t* __restrict__ part, uint32_t* __restrict__ out) {
+    __shared__ uint32_t wsum[kScanThreads / 32];
+    int M = vs->n - minus;
+    size_t base = (size_t)blockIdx.x * kScanTile + (size_t)threadIdx.x * kScanItems;
+    uint32_t v[kScanItems], local = 0;
+#pragma unroll
+    for (int r = 0; r < kScanItems; ++r) {
+        size_t i = base + r;
+        v[r] = (long long)i < M ? in[i] : 0u;
+        local += v[r];
+    }
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = local;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) wsum[warp] = incl;
+    __syncthreads();
+    uint32_t woff = 0;
+    for (int w = 0; w < warp; ++w) woff += wsum[w];
+    uint32_t run = part[blockIdx.x] + woff + incl - local;
+#pragma unroll
+    for (int r = 0; r < kScanItems; ++r) {
+        size_t i = base + r;
+        if ((long long)i < M) out[i] = run;
+        run += v[r];
+    }
+}
+
+// ---------------------------------------------------- 4 leaves + Karras
+__device__ __forceinline__ float trunc_radius(float h, float precision, int count) {
+    return fsqrt(fmul(fmul(-2.0f, fmul(h, h)), det_logf(fdiv(precision, (float)(unsigned)count))));
+}
+
+__global__ void k_leaves(int N, float W, float H, float f, const float* __restrict__ pts,
+                         const ViewState* vs, float precision, const uint32_t* __restrict__ ids,
+                         float2* __restrict__ leaf_xy, int* __restrict__ leaf_id, int4* __restrict__ lnk,
+                         int* __restrict__ par, float4* __restrict__ box, float4* __restrict__ cen) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int n = vs->n;
+    if (i >= n) return;
+    int id = (int)ids[i];
+    float p[3] = {pts[3 * (size_t)id], pts[3 * (size_t)id + 1], pts[3 * (size_t)id + 2]};
+    float s[2];
+    screen_point(W, H, f, p, s);
+    int v = n - 1 + i;
+    leaf_xy[i] = make_float2(s[0], s[1]);
+    leaf_id[i] = id;
+    lnk[v] = make_int4(-1, -1, i, 1);
+    par[v] = -1;
+    box[v] = make_float4(s[0], s[1], s[0], s[1]);
+    cen[v] = make_float4(s[0], s[1], trunc_radius(vs->h, precision, 1), make_meta(0, 0));
+}
+
+__device__ __forceinline__ int cpref(const uint32_t* keys, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    unsigned long long a = ((unsigned long long)keys[i] << 32) | (unsigned)i;
+    unsigned long long b = ((unsigned long long)keys[j] << 32) | (unsigned)j;
+    return __clzll(a ^ b);
+}
+
+// determineRange / findSplit (buildRadixTree.cuh:76-167), Karras (2012)
+__global__ void k_karras(const ViewState* vs, const uint32_t* __restrict__ keys, int4* __restrict__ lnk,
+                         int* __restrict__ par) {
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    int n = vs->n;
+    if (idx >= n - 1) return;
+    int lo, hi;
+    if (idx == 0) {
+        lo = 0; hi = n - 1;
+        par[0] = -1;
+    } else {
+        int dL = cpref(keys, n, idx, idx - 1), dR = cpref(keys, n, idx, idx + 1);
+        int d = (dR > dL) ? 1 : -1;
+        int dmin = min(dL, dR);
+        int lmax = 2;
+        while (cpref(keys, n, idx, idx + d * lmax) > dmin) lmax <<= 1;
+        int l = 0;
+        for (int t = lmax >> 1; t > 0; t >>= 1)
+            if (cpref(keys, n, idx, idx + (l + t) * d) > dmin) l += t;
+        int j = idx + l * d;
+        lo = d < 0 ? j : idx;
+        hi = d < 0 ? idx : j;
+    }
+    int dnode = cpref(keys, n, lo, hi);
+    int split = lo, stride = hi - lo;
+    do {
+        stride = (stride + 1) >> 1;
+        int mid = split + stride;
+        if (mid < hi && cpref(keys, n, lo, mid) > dnode) split = mid;
+    } while (stride > 1);
+    int lc = split, rc = split + 1;
+    if (lo == split) lc += n - 1;
+    if (hi == split + 1) rc += n - 1;
+    lnk[idx] = make_int4(lc, rc, lo, hi - lo + 1);
+    par[lc] = idx;
+    par[rc] = idx;
+}
+
+// ------------------------------------------------------------ 5 bottom-up
+// hermiteError (hermitefmm.cuh:184-195) with integer powers as products
+__device__ __forceinline__ float hermite_error(float r, float nr, unsigned ph) {
+    if (r >= 1.0f) return r;
+    float om = fsub(1.0f, r);
+    float a = fdiv(nr, fmul(om, om));
+    float rp = ipowf(r, ph);
+    float b = fdiv(rp, fsqrt(facf(ph)));
+    float c = fmul(b, b);
+    float d = fmul(fmul(2.0f, fsub(1.0f, rp)), b);
+    return fmul(a, fadd(c, d));
+}
+
+// InternalNodeFunctor (buildDynamicRadixTree.cuh:155-221): the second thread
+// to reach a node merges it.  Child centres are read at [child] (the
+// reference indexes expansionPoints[child] instead of [2*child]).
+__global__ void k_bottomup(const ViewState* vs, float precision, int max_degree,
+                           const int4* __restrict__ lnk, const int* __restrict__ par, float4* box,
+                           float4* cen, unsigned* fanin) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int n = vs->n;
+    if (i >= n || n < 2) return;
+    float h = vs->h;
+    int v = n - 1 + i;
+    while (true) {
+        int p = par[v];
+        if (p < 0) break;
+        __threadfence();
+        unsigned old = atomicAdd(&fanin[p], 1u);
+        if (old == 0) return;
+        __threadfence();
+        int4 L = lnk[p];
+        int a = L.x, b = L.y;
+        float4 ba = __ldcg(&box[a]), bb = __ldcg(&box[b]);
+        float4 ca = __ldcg(&cen[a]), cb = __ldcg(&cen[b]);
+        float na = (float)(unsigned)lnk[a].w, nb = (float)(unsigned)lnk[b].w, nc = (float)(unsigned)L.w;
+        float4 bx = make_float4(fminf(ba.x, bb.x), fminf(ba.y, bb.y), fmaxf(ba.z, bb.z), fmaxf(ba.w, bb.w));
+        float cx = fdiv(fadd(fmul(na, ca.x), fmul(nb, cb.x)), nc);
+        float cy = fdiv(fadd(fmul(na, ca.y), fmul(nb, cb.y)), nc);
+        float mn = fmaxf(0.0f, fmaxf(fsub(cx, bx.x), fsub(bx.z, cx)));
+        mn = fmaxf(mn, fmaxf(fsub(cy, bx.y), fsub(bx.w, cy)));
+        float r = fdiv(mn, h);
+        int d0 = max(meta_degree(ca.w), meta_degree(cb.w));
+        unsigned deg = (unsigned)max(d0, 0);
+        while (deg <= (unsigned)max_degree && hermite_error(r, nc, deg) > precision && r < 1.0f) deg += 1;
+        int degree = (r < 1.0f && deg <= (unsigned)max_degree) ? (int)deg : -1;
+        __stcg(&box[p], bx);
+        __stcg(&cen[p], make_float4(cx, cy, trunc_radius(h, precision, L.w), make_meta(0, degree)));
+        v = p;
+    }
+}
+
+// ------------------------------------------------ 6 coefficient offsets
+__global__ void k_node_sizes(const ViewState* vs, const float4* __restrict__ cen, uint32_t* __restrict__ sizes) {
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= vs->n - 1) return;
+    int d = meta_degree(cen[v].w);
+    sizes[v] = d >= 0 ? (uint32_t)((d + 1) * (d + 1)) : 0u;
+}
+
+__global__ void k_assign(ViewState* vs, float4* cen, const uint32_t* __restrict__ sizes,
+                         const uint32_t* __restrict__ offsets, size_t cap, uds_view_stats* st) {
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    int n = vs->n;
+    if (v >= n - 1) return;
+    uint32_t sz = sizes[v];
+    if (sz == 0) return;
+    float4 c = cen[v];
+    int d = meta_degree(c.w);
+    uint32_t off = offsets[v];
+    if ((size_t)off + sz > cap) {
+        c.w = make_meta(0, -1);
+        atomicAdd(&st->demoted, 1);
+    } else {
+        c.w = make_meta((int)off, d);
+        atomicMax(&vs->coef_used, off + sz);
+    }
+    cen[v] = c;
+}
+
+// ----------------------------------------------------------------- 7 P2M
+// shiftLeafHermiteExpansion (hermitefmm.cuh:119-138) summed per node over
+// its leaves in Morton order.  One warp per internal node.
+__global__ void k_p2m(const ViewState* vs, const int4* __restrict__ lnk, const float4* __restrict__ cen,
+                      const float2* __restrict__ leaf_xy, float* __restrict__ coef) {
+    int v = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    int lane = threadIdx.x & 31;
+    if (v >= vs->n - 1) return;
+    float4 c = cen[v];
+    int p = meta_degree(c.w);
+    if (p < 0) return;
+    int off = meta_offset(c.w);
+    int4 L = lnk[v];
+    float sq = vs->sq;
+    int P1 = p + 1;
+    for (int k = lane; k < P1 * P1; k += 32) {
+        unsigned a = (unsigned)(k / P1), b = (unsigned)(k % P1);
+        float fab = fmul(facf(a), facf(b));
+        float sum = 0.0f;
+        for (int i = L.z; i < L.z + L.w; ++i) {
+            float2 q = leaf_xy[i];
+            float s0 = fdiv(fsub(q.x, c.x), sq);
+            float s1 = fdiv(fsub(q.y, c.y), sq);
+            float term = fdiv(fmul(1.0f, fmul(ipowf(s0, a), ipowf(s1, b))), fab);
+            sum = fadd(sum, term);
+        }
+        coef[off + k] = sum;
+    }
+}
+
+// -------------------------------------------------------- FGT evaluation
+struct Tree {
+    const int4* lnk;
+    const int* par;
+    const float4* box;
+    const float4* cen;
+    const float* coef;
+    const float2* leaf_xy;
+    const int* leaf_id;
+    int n;
+    float sq;
+};
+
+// evluateHermite with hermiteFunction (hermitefmm.cuh:35-47, 213-237)
+__device__ __forceinline__ float hermite_eval(const Tree& T, int v, float4 c, float qx, float qy) {
+    float tx = fdiv(fsub(qx, c.x), T.sq);
+    float ty = fdiv(fsub(qy, c.y), T.sq);
+    float ex = det_expf(-fmul(tx, tx));
+    float ey = det_expf(-fmul(ty, ty));
+    if (v >= T.n - 1) return fadd(0.0f, fmul(fmul(1.0f, ex), ey));
+    int p = meta_degree(c.w);
+    const float* C = T.coef + meta_offset(c.w);
+    float hy[kMaxDegree + 1];
+    float ty2 = fmul(2.0f, ty);
+    hy[0] = ey;
+    hy[1] = fmul(ty2, ey);
+#pragma unroll
+    for (int k = 2; k <= kMaxDegree; ++k)
+        if (k <= p) hy[k] = fsub(fmul(ty2, hy[k - 1]), fmul(fmul(2.0f, (float)(k - 1)), hy[k - 2]));
+    float tx2 = fmul(2.0f, tx);
+    float hxm2 = 0.0f, hxm1 = 0.0f, hx = ex;
+    float w = 0.0f;
+    for (int a = 0; a <= p; ++a) {
+        if (a == 1) hx = fmul(tx2, ex);
+        else if (a >= 2) hx = fsub(fmul(tx2, hxm1), fmul(fmul(2.0f, (float)(a - 1)), hxm2));
+        const float* Ca = C + a * (p + 1);
+#pragma unroll
+        for (int b = 0; b <= kMaxDegree; ++b)
+            if (b <= p) w = fadd(w, fmul(fmul(Ca[b], hx), hy[b]));
+        hxm2 = hxm1;
+        hxm1 = hx;
+    }
+    return w;
+}
+
+__device__ __forceinline__ bool truncated(const Tree& T, int v, float r, float qx, float qy) {
+    float4 b = T.box[v];
+    float clx = fminf(fmaxf(qx, b.x), b.z), cly = fminf(fmaxf(qy, b.y), b.w);
+    float dx = fsub(qx, clx), dy = fsub(qy, cly);
+    float d2 = fadd(fadd(0.0f, fmul(dx, dx)), fmul(dy, dy));
+    return !(d2 < fmul(r, r));
+}
+
+// getWeight / accumulateSubtree (evaluateDynamicRadixTree.cuh:129-242)
+__device__ float node_weight(const Tree& T, int v, float qx, float qy) {
+    float4 c = T.cen[v];
+    if (meta_degree(c.w) >= 0) return hermite_eval(T, v, c, qx, qy);
+    int rootparent = T.par[v];
+    float w = 0.0f;
+    do {
+        c = T.cen[v];
+        while (meta_degree(c.w) < 0 && !truncated(T, v, c.z, qx, qy)) {
+            v = T.lnk[v].x;
+            c = T.cen[v];
+        }
+        if (meta_degree(c.w) >= 0) w = fadd(w, hermite_eval(T, v, c, qx, qy));
+        int p = T.par[v];
+        while (p != rootparent && v == T.lnk[p].y) {
+            v = p;
+            p = T.par[p];
+        }
+        if (p != rootparent) v = T.lnk[p].y;
+    } while (T.par[v] != rootparent);
+    return w;
+}
+
+// --------------------------------------------------------------- 8 sampler
+template <int R, int KM>
+__global__ void __launch_bounds__(128) k_sample(Tree T, const ViewState* vs, int W, int H, int K,
+                                                float precision, const float* __restrict__ uniforms,
+                                                uint64_t seed, uint32_t view, int* __restrict__ indices,
+                                                uds_view_stats* st) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    int i = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= W || j >= H) return;
+    T.n = vs->n;
+    T.sq = vs->sq;
+    size_t pixel = (size_t)j + (size_t)H * i;
+    int* out = indices + (size_t)K * pixel;
+    if (T.n == 0) return;  // indices were preset to -1
+    float qx = (float)i, qy = (float)j;
+    float total = fmaxf(0.0f, node_weight(T, 0, qx, qy));
+    if (total < precision) return;
+    int ids[KM];
+    float keys[KM];
+    for (int k = 0; k < K; ++k) { ids[k] = -1; keys[k] = __int_as_float(0x7f800000); }
+    int tn[R][kTrace];
+    float tc[R][kTrace];
+    float tp[kTrace];
+    int tl[R];
+    float u[KM];
+    bool overflow = false;
+    for (int r = 0; r < R; ++r) {
+        if (uniforms) {
+            const float* up = uniforms + ((size_t)pixel * R + r) * K;
+            for (int k = 0; k < K; ++k) u[k] = up[k];
+        } else {
+            int G = (K + 3) >> 2;
+            for (int g = 0; g < G; ++g) {
+                uint32_t c4[4] = {(uint32_t)pixel, view, (uint32_t)(r * G + g), 0u};
+                philox4x32_10(c4, (uint32_t)seed, (uint32_t)(seed >> 32));
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if (4 * g + q < K) u[4 * g + q] = bits_to_uniform(c4[q]);
+            }
+        }
+        int v = 0, d = 0;
+        tn[r][0] = 0;
+        tp[0] = 1.0f;
+        int4 L = T.lnk[0];
+        while (L.w > K) {
+            int a = L.x, b = L.y;
+            float w0 = fmaxf(0.0f, node_weight(T, a, qx, qy));
+            float w1 = fmaxf(0.0f, node_weight(T, b, qx, qy));
+            float sum = fadd(fadd(0.0f, w0), w1);
+            w0 = fdiv(w0, sum);
+            w1 = fdiv(w1, sum);
+            float c0 = 1.0f, c1 = 1.0f;
+            for (int rr = r - 1; rr >= 0; --rr)
+                if (d + 1 < tl[rr] && tn[rr][d + 1] == a) { c0 = tc[rr][d + 1]; break; }
+            for (int rr = r - 1; rr >= 0; --rr)
+                if (d + 1 < tl[rr] && tn[rr][d + 1] == b) { c1 = tc[rr][d + 1]; break; }
+            float s0 = fmul(w0, c0), s1 = fmul(w1, c1);
+            ++d;
+            if (d >= kTrace) { overflow = true; break; }
+            if (s0 < s1) { tn[r][d] = b; tp[d] = w1; v = b; }
+            else { tn[r][d] = a; tp[d] = w0; v = a; }
+            L = T.lnk[v];
+        }
+        if (overflow) break;
+        tl[r] = d + 1;
+        float prob = 1.0f;
+        for (int m = d; m >= 0; --m) {
+            float cap = 1.0f;
+            for (int rr = r - 1; rr >= 0; --rr)
+                if (m < tl[rr] && tn[rr][m] == tn[r][m]) { cap = tc[rr][m]; break; }
+            tc[r][m] = fmaxf(0.0f, fsub(cap, prob));
+            prob = fmul(prob, tp[m]);
+        }
+        // order sampling over the subtree's leaves (insertSample,
+        // sequentialPoissonRadixTree.cuh:15-41)
+        int f0 = L.z, cnt = L.w;
+        for (int k = 0; k < cnt; ++k) {
+            int leafNode = T.n - 1 + f0 + k;
+            float pw = fmaxf(0.0f, node_weight(T, leafNode, qx, qy));
+            float key = fdiv(u[k], pw);
+            int index = T.leaf_id[f0 + k];
+            for (int q = 0; q < K; ++q) {
+                if (key < keys[q]) {
+                    int ti = ids[q]; ids[q] = index; index = ti;
+                    float tk = keys[q]; keys[q] = key; key = tk;
+                }
+                if (index == -1) break;
+            }
+        }
+    }
+    if (overflow) atomicAdd(&st->overflow, 1);
+    for (int k = 0; k < K; ++k) out[k] = ids[k];
+}
+
+__global__ void k_finish_view(const ViewState* vs, uds_view_stats* st) {
+    st->n_visible = vs->n;
+    st->n_coefs = (int)vs->coef_used;
+}
+
+// Evaluate getWeight for (node, query) pairs (debug entry point).
+__global__ void k_fgt_eval(Tree T, const ViewState* vs, int m, const int* __restrict__ nodes,
+                           const float* __restrict__ q, float* __restrict__ out) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= m) return;
+    T.n = vs->n;
+    T.sq = vs->sq;
+    out[t] = node_weight(T, nodes[t], q[2 * t], q[2 * t + 1]);
+}
+
+// ------------------------------------------------------------ host side
+static int build_view(const uds_sample_params* p, const Ws& w, int view, const float* pts,
+                      const float* nrm, const float* sd, const float* h_override, cudaStream_t s) {
+    int N = p->N;
+    float W = (float)p->W, H = (float)p->H, f = p->focal;
+    const float* vp = pts + 3 * (size_t)N * view;
+    const float* vn = nrm + 3 * (size_t)N * view;
+    const float* vsd = sd + (p->std_batch > 1 ? 2 * (size_t)N * view : 0);
+    cudaError_t e = cudaMemsetAsync(w.vs, 0, sizeof(ViewState), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(w.fanin, 0, 4 * (size_t)(N > 0 ? N : 1), s);
+    if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
+    int st;
+    unsigned nbN = cdiv(N > 0 ? N : 1, 128);
+    if (N > 0) {
+        k_bandwidth<<<nbN, 128, 0, s>>>(N, W, H, f, vp, vn, vsd, p->smoothing, w.vs);
+        if ((st = launch_status())) return st;
+    }
+    k_view_setup<<<1, 1, 0, s>>>(h_override, view, W, H, p->precision, w.vs, w.stats);
+    if ((st = launch_status())) return st;
+    if (N == 0) return UDS_OK;
+    k_cull_morton<<<nbN, 128, 0, s>>>(N, W, H, f, vp, w.vs, w.keysA, w.idsA);
+    if ((st = launch_status())) return st;
+    unsigned nb = cdiv(N, kSortTile);
+    uint32_t *ki = w.keysA, *vi = w.idsA, *ko = w.keysB, *vo = w.idsB;
+    for (int pass = 0; pass < 4; ++pass) {
+        int shift = 8 * pass;
+        k_radix_hist<<<nb, kSortThreads, 0, s>>>(N, ki, shift, w.hist);
+        k_radix_scan<<<1, 1024, 0, s>>>(w.hist, (int)(256 * nb));
+        k_radix_scatter<<<nb, kSortThreads, 0, s>>>(N, ki, vi, ko, vo, shift, w.hist);
+        if ((st = launch_status())) return st;
+        uint32_t* t = ki; ki = ko; ko = t;
+        t = vi; vi = vo; vo = t;
+    }
+    // after an even number of passes the sorted data is back in A
+    k_leaves<<<nbN, 128, 0, s>>>(N, W, H, f, vp, w.vs, p->precision, vi, w.leaf_xy, w.leaf_id, w.lnk, w.par,
+                                 w.box, w.cen);
+    k_karras<<<nbN, 128, 0, s>>>(w.vs, ki, w.lnk, w.par);
+    k_bottomup<<<nbN, 128, 0, s>>>(w.vs, p->precision, p->max_degree, w.lnk, w.par, w.box, w.cen, w.fanin);
+    k_node_sizes<<<nbN, 128, 0, s>>>(w.vs, w.cen, w.sizes);
+    if ((st = launch_status())) return st;
+    unsigned sb = cdiv(N, kScanTile);
+    k_scan_reduce<<<sb, kScanThreads, 0, s>>>(w.sizes, w.vs, 1, w.scanTmp);
+    k_scan_top<<<1, 1024, 0, s>>>(w.scanTmp, (int)sb);
+    k_scan_down<<<sb, kScanThreads, 0, s>>>(w.sizes, w.vs, 1, w.scanTmp, w.offsets);
+    k_assign<<<nbN, 128, 0, s>>>(w.vs, w.cen, w.sizes, w.offsets, w.coef_cap, w.stats + view);
+    k_p2m<<<cdiv((size_t)N * 32, 128), 128, 0, s>>>(w.vs, w.lnk, w.cen, w.leaf_xy, w.coef);
+    k_finish_view<<<1, 1, 0, s>>>(w.vs, w.stats + view);
+    return launch_status();
+}
+
+static Tree tree_of(const Ws& w) {
+    Tree T;
+    T.lnk = w.lnk; T.par = w.par; T.box = w.box; T.cen = w.cen; T.coef = w.coef;
+    T.leaf_xy = w.leaf_xy; T.leaf_id = w.leaf_id; T.n = 0; T.sq = 0.0f;
+    return T;
+}
+
+template <int R>
+static void launch_sample(const Tree& T, const Ws& w, const uds_sample_params* p, const float* u, int view,
+                          int* idx, cudaStream_t s) {
+    dim3 block(32, 4);
+    dim3 grid(cdiv(p->H, block.x), cdiv(p->W, block.y));
+    if (p->K <= 8)
+        k_sample<R, 8><<<grid, block, 0, s>>>(T, w.vs, p->W, p->H, p->K, p->precision, u, p->seed, (uint32_t)view,
+                                              idx, w.stats + view);
+    else
+        k_sample<R, kMaxK><<<grid, block, 0, s>>>(T, w.vs, p->W, p->H, p->K, p->precision, u, p->seed,
+                                                  (uint32_t)view, idx, w.stats + view);
+}
+
+static int check_params(const uds_sample_params* p) {
+    if (!p) return UDS_ERR_ARGUMENT;
+    if (p->B <= 0 || p->N < 0 || p->W <= 0 || p->H <= 0 || p->K <= 0 || p->K > kMaxK) return UDS_ERR_ARGUMENT;
+    if (p->max_degree < 0 || p->max_degree > kMaxDegree) return UDS_ERR_ARGUMENT;
+    if (p->std_batch != 1 && p->std_batch != p->B) return UDS_ERR_ARGUMENT;
+    if (!(p->precision > 0.0f) || !(p->focal > 0.0f)) return UDS_ERR_ARGUMENT;
+    if ((size_t)p->N * 2 >= (1u << 31)) return UDS_ERR_ARGUMENT;
+    int64_t pool = p->coef_pool > 0 ? p->coef_pool : default_pool(p->N);
+    if (pool >= (1ll << 26)) return UDS_ERR_ARGUMENT;  // offsets are packed in 26 bits
+    return UDS_OK;
+}
+
+}  // namespace uds
+
+using namespace uds;
+
+extern "C" size_t uds_sample_workspace_size(const uds_sample_params* prm) {
+    if (check_params(prm)) return 0;
+    return layout(prm, nullptr).bytes;
+}
+
+extern "C" int uds_sample(const uds_sample_params* prm, const float* points, const float* normals,
+                          const float* std_devs, const float* uniforms, const float* h_override,
+                          int32_t* indices, uds_view_stats* stats, void* workspace, size_t workspace_bytes,
+                          void* stream) {
+    int st = check_params(prm);
+    if (st) return st;
+    if (!indices || (prm->N > 0 && (!points || !normals || !std_devs))) return UDS_ERR_ARGUMENT;
+    Ws w = layout(prm, reinterpret_cast<char*>(workspace));
+    if (!workspace || workspace_bytes < w.bytes) return UDS_ERR_WORKSPACE;
+    cudaStream_t s = as_stream(stream);
+    size_t per_view = (size_t)prm->W * prm->H * prm->K;
+    cudaError_t e = cudaMemsetAsync(indices, 0xFF, sizeof(int32_t) * per_view * prm->B, s);
+    if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
+    int R = num_rounds(prm->K);
+    Tree T = tree_of(w);
+    for (int b = 0; b < prm->B; ++b) {
+        if ((st = build_view(prm, w, b, points, normals, std_devs, h_override, s))) return st;
+        if (prm->N == 0) continue;
+        const float* u = uniforms ? uniforms + per_view / prm->K * R * prm->K * b : nullptr;
+        int* idx = indices + per_view * b;
+        switch (R) {
+            case 1: launch_sample<1>(T, w, prm, u, b, idx, s); break;
+            case 2: launch_sample<2>(T, w, prm, u, b, idx, s); break;
+            case 3: launch_sample<3>(T, w, prm, u, b, idx, s); break;
+            case 4: launch_sample<4>(T, w, prm, u, b, idx, s); break;
+            case 5: launch_sample<5>(T, w, prm, u, b, idx, s); break;
+            case 6: launch_sample<6>(T, w, prm, u, b, idx, s); break;
+            case 7: launch_sample<7>(T, w, prm, u, b, idx, s); break;
+            default: launch_sample<8>(T, w, prm, u, b, idx, s); break;
+        }
+        if ((st = launch_status())) return st;
+    }
+    if (stats) {
+        e = cudaMemcpyAsync(stats, w.stats, sizeof(uds_view_stats) * prm->B, cudaMemcpyDeviceToDevice, s);
+        if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
+    }
+    return UDS_OK;
+}
+
+extern "C" int uds_tree_build(const uds_sample_params* prm, int view, const float* points,
+                              const float* normals, const float* std_devs, const float* h_override,
+                              uds_view_stats* stats, uint32_t* keys, int32_t* ids, int32_t* left,
+                              int32_t* right, int32_t* parent, int32_t* count, int32_t* degree, float* centre,
+                              float* box, void* workspace, size_t workspace_bytes, void* stream);
+
+namespace uds {
+// Copy the built tree into plain per-node arrays (debug).
+__global__ void k_export(const ViewState* vs, const Ws w, uint32_t* keys, int* ids, int* left, int* right,
+                         int* parent, int* count, int* degree, float* centre, float* box) {
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    int n = vs->n;
+    int M = n > 0 ? 2 * n - 1 : 0;
+    if (v < n) {
+        if (keys) keys[v] = w.keysA[v];
+        if (ids) ids[v] = w.leaf_id[v];
+    }
+    if (v < M) {
+        int4 L = w.lnk[v];
+        float4 c = w.cen[v], b = w.box[v];
+        if (left) left[v] = L.x;
+        if (right) right[v] = L.y;
+        if (parent) parent[v] = w.par[v];
+        if (count) count[v] = L.w;
+        if (degree) degree[v] = meta_degree(c.w);
+        if (centre) { centre[2 * v] = c.x; centre[2 * v + 1] = c.y; }
+        if (box) { box[4 * v] = b.x; box[4 * v + 1] = b.y; box[4 * v + 2] = b.z; box[4 * v + 3] = b.w; }
+    }
+}
+}  // namespace uds
+
+extern "C" int uds_tree_build(const uds_sample_params* prm, int view, const float* points,
+                              const float* normals, const float* std_devs, const float* h_override,
+                              uds_view_stats* stats, uint32_t* keys, int32_t* ids, int32_t* left,
+                              int32_t* right, int32_t* parent, int32_t* count, int32_t* degree, float* centre,
+                              float* box, void* workspace, size_t workspace_bytes, void* stream) {
+    int st = check_params(prm);
+    if (st) return st;
+    if (view < 0 || view >= prm->B) return UDS_ERR_ARGUMENT;
+    Ws w = layout(prm, reinterpret_cast<char*>(workspace));
+    if (!workspace || workspace_bytes < w.bytes) return UDS_ERR_WORKSPACE;
+    cudaStream_t s = as_stream(stream);
+    if ((st = build_view(prm, w, view, points, normals, std_devs, h_override, s))) return st;
+    if (prm->N > 0) {
+        k_export<<<cdiv(2 * (size_t)prm->N, 128), 128, 0, s>>>(w.vs, w, keys, ids, left, right, parent, count,
+                                                               degree, centre, box);
+        if ((st = launch_status())) return st;
+    }
+    if (stats) {
+        cudaError_t e = cudaMemcpyAsync(stats, w.stats + view, sizeof(uds_view_stats), cudaMemcpyDeviceToDevice, s);
+        if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
+    }
+    return UDS_OK;
+}
+
+extern "C" int uds_fgt_eval(const uds_sample_params* prm, int m, const int32_t* nodes, const float* query_xy,
+                            float* out, const void* workspace, size_t workspace_bytes, void* stream) {
+    int st = check_params(prm);
+    if (st) return st;
+    Ws w = layout(prm, reinterpret_cast<char*>(const_cast<void*>(workspace)));
+    if (!workspace || workspace_bytes < w.bytes) return UDS_ERR_WORKSPACE;
+    if (m <= 0) return UDS_OK;
+    k_fgt_eval<<<cdiv(m, 128), 128, 0, as_stream(stream)>>>(tree_of(w), w.vs, m, nodes, query_xy, out);
+    return launch_status();
+}

@@ -1,0 +1,116 @@
+// Batched 4x4 affine / linear transform of splat vectors and its backward
+// (transform.cpp:33-86, transformCuda.cu:11-117, transformation.cuh:8-27).
+#include "uds_common.cuh"
+
+namespace uds {
+
+// Camera-space transform with the reference's summation order
+// ((0 + m0 p0) + m1 p1) + m2 p2 (+ m3), exact rounding: the result feeds the
+// bit-exact sampler.
+template <bool Affine>
+__global__ void k_transform_forward(int B, const float* __restrict__ M, int vB, int N,
+                                    const float* __restrict__ v, float* __restrict__ out) {
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    int b = blockIdx.y;
+    if (x >= N) return;
+    const float* T = M + 16 * b;
+    const float* p = v + 3 * ((size_t)x + (vB > 1 ? (size_t)N * b : 0));
+    float p0 = p[0], p1 = p[1], p2 = p[2];
+    float* o = out + 3 * ((size_t)x + (size_t)N * b);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        float s = fadd(fadd(fadd(0.0f, fmul(T[4 * i], p0)), fmul(T[4 * i + 1], p1)), fmul(T[4 * i + 2], p2));
+        if (Affine) s = fadd(s, T[4 * i + 3]);
+        o[i] = s;
+    }
+}
+
+// gM[b] = sum_x g_x (v_x, 1)^T (row 3 stays zero); block-reduced then one
+// atomic per entry and block.  gv[x] = sum_b M_b^T g_bx (loops over b when
+// the vectors are broadcast, so no atomics on gv).
+template <bool Affine>
+__global__ void k_transform_backward(int B, const float* __restrict__ grad,
+                                     const float* __restrict__ M, int vB, int N,
+                                     const float* __restrict__ v, float* __restrict__ gM,
+                                     float* __restrict__ gv) {
+    __shared__ float red[12][32];
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    int b = blockIdx.y;
+    float acc[12];
+#pragma unroll
+    for (int i = 0; i < 12; ++i) acc[i] = 0.0f;
+    if (x < N) {
+        const float* g = grad + 3 * ((size_t)x + (size_t)N * b);
+        const float* p = v + 3 * ((size_t)x + (vB > 1 ? (size_t)N * b : 0));
+        float g0 = g[0], g1 = g[1], g2 = g[2];
+        float gg[3] = {g0, g1, g2};
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            acc[4 * i + 0] = gg[i] * p[0];
+            acc[4 * i + 1] = gg[i] * p[1];
+            acc[4 * i + 2] = gg[i] * p[2];
+            acc[4 * i + 3] = Affine ? gg[i] : 0.0f;
+        }
+        if (vB > 1 || B == 1) {
+            const float* T = M + 16 * b;
+            float* o = gv + 3 * ((size_t)x + (vB > 1 ? (size_t)N * b : 0));
+#pragma unroll
+            for (int j = 0; j < 3; ++j) o[j] = g0 * T[j] + g1 * T[4 + j] + g2 * T[8 + j];
+        } else if (b == 0) {
+            float r[3] = {0.0f, 0.0f, 0.0f};
+            for (int bb = 0; bb < B; ++bb) {
+                const float* T = M + 16 * bb;
+                const float* gb = grad + 3 * ((size_t)x + (size_t)N * bb);
+#pragma unroll
+                for (int j = 0; j < 3; ++j) r[j] += gb[0] * T[j] + gb[1] * T[4 + j] + gb[2] * T[8 + j];
+            }
+            float* o = gv + 3 * (size_t)x;
+#pragma unroll
+            for (int j = 0; j < 3; ++j) o[j] = r[j];
+        }
+    }
+    // block reduction: warp shuffle, then across warps
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < 12; ++i) {
+        float a = acc[i];
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if (lane == 0) red[i][warp] = a;
+    }
+    __syncthreads();
+    if (threadIdx.x < 12) {
+        float a = 0.0f;
+        int nw = blockDim.x >> 5;
+        for (int w = 0; w < nw; ++w) a += red[threadIdx.x][w];
+        int i = threadIdx.x;
+        if (Affine || (i & 3) != 3) atomicAdd(&gM[16 * b + i], a);
+    }
+}
+
+}  // namespace uds
+
+using namespace uds;
+
+extern "C" int uds_transform_forward(int affine, int B, const float* M, int vB, int N,
+                                     const float* v, float* out, void* stream) {
+    if (B <= 0 || N < 0 || (vB != 1 && vB != B) || !M || (N > 0 && (!v || !out))) return UDS_ERR_ARGUMENT;
+    if (N == 0) return UDS_OK;
+    dim3 grid(cdiv(N, 256), B);
+    if (affine) k_transform_forward<true><<<grid, 256, 0, as_stream(stream)>>>(B, M, vB, N, v, out);
+    else k_transform_forward<false><<<grid, 256, 0, as_stream(stream)>>>(B, M, vB, N, v, out);
+    return launch_status();
+}
+
+extern "C" int uds_transform_backward(int affine, int B, const float* grad, const float* M, int vB,
+                                      int N, const float* v, float* gM, float* gv, void* stream) {
+    if (B <= 0 || N < 0 || (vB != 1 && vB != B) || !M || !gM || (N > 0 && (!grad || !v || !gv)))
+        return UDS_ERR_ARGUMENT;
+    cudaStream_t s = as_stream(stream);
+    cudaError_t e = cudaMemsetAsync(gM, 0, sizeof(float) * 16 * (size_t)B, s);
+    if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
+    if (N == 0) return UDS_OK;
+    dim3 grid(cdiv(N, 256), B);
+    if (affine) k_transform_backward<true><<<grid, 256, 0, s>>>(B, grad, M, vB, N, v, gM, gv);
+    else k_transform_backward<false><<<grid, 256, 0, s>>>(B, grad, M, vB, N, v, gM, gv);
+    return launch_status();
+}

@@ -1,0 +1,143 @@
+"""cudaExtensions.sampling (sampling.cpp:48-94, samplingCuda.cu:197-321).
+
+``sample`` builds, per view, the FMM tree over the projected splat centres and
+draws ``numSamples`` splat indices per pixel by the sequential-Poisson tree
+descent.  Additions over the reference, all optional keyword arguments at the
+end so existing calls keep working:
+
+* ``uniforms``: (B,W,H,R,K) float32 in (0,1], R = ceil(sqrt(K)), the random
+  numbers consumed by the order sampling (round-major per pixel, candidates in
+  Morton order).  Without it Philox4x32-10 uniforms are drawn from ``seed``
+  (the reference seeds curand with time(NULL)).
+* ``seed``: 64-bit Philox key; default draws one from torch's CPU generator.
+* ``h``: (B,) float32 CUDA tensor of bandwidths that replace the computed ones
+  (entries <= 0 keep the computed value).
+* ``return_stats``: also return the per-view record (h, cull radius, visible
+  splats, stored coefficients, demoted nodes, trace overflows) as a (B,8)
+  tensor viewed from uds_view_stats.
+"""
+from __future__ import annotations
+
+import math
+
+import torch
+
+from .._lib import SampleParams, Workspace, check, load, need, ptr, stream_ptr
+
+MAX_DEGREE = 16
+
+
+def num_rounds(K: int) -> int:
+    return int(math.ceil(math.sqrt(K) - 1e-12))
+
+
+def params(width, height, focallength, points, stdDevs, numSamples, smoothing, precision, seed=0,
+           max_degree=MAX_DEGREE, coef_pool=0) -> SampleParams:
+    return SampleParams(B=points.shape[0], N=points.shape[1], W=int(width), H=int(height), K=int(numSamples),
+                        focal=float(focallength), smoothing=float(smoothing), precision=float(precision),
+                        max_degree=int(max_degree), std_batch=stdDevs.shape[0], coef_pool=int(coef_pool or 0),
+                        seed=int(seed) & 0xFFFFFFFFFFFFFFFF)
+
+
+def workspace_bytes(prm: SampleParams) -> int:
+    n = load().uds_sample_workspace_size(prm)
+    if n == 0:
+        raise ValueError("invalid sampling parameters")
+    return n
+
+
+def _check(points, normals, stdDevs):
+    need(points, "points")
+    need(normals, "normals", device=points.device)
+    need(stdDevs, "stdDevs", device=points.device)
+    if points.dim() != 3 or points.shape[2] != 3 or normals.shape != points.shape:
+        raise ValueError("points and normals must be (B,N,3)")
+    if stdDevs.dim() != 3 or stdDevs.shape[2] != 2 or stdDevs.shape[1] != points.shape[1] or \
+            stdDevs.shape[0] not in (1, points.shape[0]):
+        raise ValueError("stdDevs must be (1|B,N,2)")
+
+
+def sample(width: int, height: int, focallength: float, points, normals, colors, stdDevs, numSamples: int,
+           smoothing: float, precision: float, uniforms=None, seed=None, h=None, return_stats=False,
+           max_degree=MAX_DEGREE, coef_pool=0):
+    _check(points, normals, stdDevs)
+    dev = points.device
+    B = points.shape[0]
+    K = int(numSamples)
+    if seed is None:
+        seed = int(torch.randint(0, 2 ** 62, (1,)).item())
+    prm = params(width, height, focallength, points, stdDevs, K, smoothing, precision, seed, max_degree, coef_pool)
+    if uniforms is not None:
+        need(uniforms, "uniforms", device=dev)
+        R = num_rounds(K)
+        if tuple(uniforms.shape) != (B, int(width), int(height), R, K):
+            raise ValueError(f"uniforms must be (B,W,H,{R},{K})")
+    if h is not None:
+        need(h, "h", device=dev)
+        if h.numel() != B:
+            raise ValueError("h must have B entries")
+    L = load()
+    ws = Workspace.get(dev, workspace_bytes(prm), "sample")
+    indices = torch.empty((B, int(width), int(height), K), dtype=torch.int32, device=dev)
+    stats = torch.empty((B, 8), dtype=torch.float32, device=dev) if return_stats else None
+    check(L.uds_sample(prm, ptr(points), ptr(normals), ptr(stdDevs), ptr(uniforms), ptr(h), ptr(indices), ptr(stats),
+                       ptr(ws), ws.numel(), stream_ptr(dev)), "sampling sample")
+    if return_stats:
+        return indices, view_stats(stats)
+    return indices
+
+
+def view_stats(stats: torch.Tensor) -> dict:
+    """Decode a (B,8) uds_view_stats tensor (synchronises)."""
+    s = stats.detach().cpu()
+    ints = s.view(torch.int32)
+    return dict(h=s[:, 0].clone(), radius=s[:, 1].clone(), n_visible=ints[:, 2].clone(), n_coefs=ints[:, 3].clone(),
+                demoted=ints[:, 4].clone(), overflow=ints[:, 5].clone())
+
+
+def build_tree(width, height, focallength, points, normals, stdDevs, numSamples, smoothing, precision, view=0,
+               h=None, max_degree=MAX_DEGREE, coef_pool=0):
+    """Build one view's tree and return its arrays (test / debug helper of
+    uds_tree_build).  Keeps the workspace for fgt_eval."""
+    _check(points, normals, stdDevs)
+    dev = points.device
+    N = points.shape[1]
+    prm = params(width, height, focallength, points, stdDevs, numSamples, smoothing, precision, 0, max_degree,
+                 coef_pool)
+    L = load()
+    ws = Workspace.get(dev, workspace_bytes(prm), "tree")
+    M = max(2 * N - 1, 1)
+    out = dict(keys=torch.empty(max(N, 1), dtype=torch.int32, device=dev),
+               ids=torch.empty(max(N, 1), dtype=torch.int32, device=dev),
+               left=torch.empty(M, dtype=torch.int32, device=dev), right=torch.empty(M, dtype=torch.int32, device=dev),
+               parent=torch.empty(M, dtype=torch.int32, device=dev), count=torch.empty(M, dtype=torch.int32, device=dev),
+               degree=torch.empty(M, dtype=torch.int32, device=dev),
+               centre=torch.empty((M, 2), dtype=torch.float32, device=dev),
+               box=torch.empty((M, 4), dtype=torch.float32, device=dev))
+    stats = torch.empty((1, 8), dtype=torch.float32, device=dev)
+    if h is not None:
+        need(h, "h", device=dev)
+    check(L.uds_tree_build(prm, int(view), ptr(points), ptr(normals), ptr(stdDevs), ptr(h), ptr(stats),
+                           ptr(out["keys"]), ptr(out["ids"]), ptr(out["left"]), ptr(out["right"]), ptr(out["parent"]),
+                           ptr(out["count"]), ptr(out["degree"]), ptr(out["centre"]), ptr(out["box"]), ptr(ws),
+                           ws.numel(), stream_ptr(dev)), "tree build")
+    st = view_stats(stats)
+    n = int(st["n_visible"][0])
+    Mn = max(2 * n - 1, 0)
+    res = {k: (v[:n] if k in ("keys", "ids") else v[:Mn]).cpu() for k, v in out.items()}
+    res["keys"] = res["keys"].view(torch.uint32) if hasattr(torch, "uint32") else res["keys"]
+    res.update({k: float(v[0]) if k in ("h", "radius") else int(v[0]) for k, v in st.items()})
+    res["_prm"] = prm
+    res["_ws"] = ws
+    return res
+
+
+def fgt_eval(tree: dict, nodes, queries):
+    """getWeight of (node, query) pairs on the tree last built by build_tree."""
+    ws = tree["_ws"]
+    nodes = need(nodes, "nodes", torch.int32)
+    queries = need(queries, "queries", device=nodes.device)
+    out = torch.empty(nodes.numel(), dtype=torch.float32, device=nodes.device)
+    check(load().uds_fgt_eval(tree["_prm"], nodes.numel(), ptr(nodes), ptr(queries), ptr(out), ptr(ws), ws.numel(),
+                              stream_ptr(nodes.device)), "fgt eval")
+    return out

@@ -1,0 +1,187 @@
+"""Autograd wrappers over the CUDA ops, with the class names, call signatures
+and gradient conventions of the reference's ``splatting/extensions/__init__.py``
+(lines 104-581) and the helpers of ``splatting/extensions/utils.py``.
+
+Gradient conventions kept from the reference:
+* ``EWASplatting.backward`` clamps each splat's point / std-dev gradient to
+  norm <= 1 (``conditionalNormalization``), zeroes NaNs and returns no gradient
+  for the normals (extensions/__init__.py:219-233);
+* ``DepthFiltering`` passes gradients only to the EWA weights;
+* the sampler runs under ``no_grad``.
+"""
+from __future__ import annotations
+
+import torch as th
+
+from .cudaExtensions import filtering, interpolation, sampling, shading, splatting, transform
+
+
+# ------------------------------------------------------------------ utils
+def normalize(x: th.Tensor, eps=1e-4) -> th.Tensor:
+    """utils.py:7-9"""
+    norm = x.norm(dim=-1, keepdim=True)
+    return x / (norm + eps)
+
+
+def dot(x: th.Tensor, y: th.Tensor, keepdim: bool) -> th.Tensor:
+    return th.sum(x.mul(y), dim=-1, keepdim=keepdim)
+
+
+def world2Camera(camPositions: th.Tensor, camQuaternion: th.Tensor) -> th.Tensor:
+    """Quaternion (x, y, z, w) + translation -> (B,1,4,4) view matrix
+    (Euler-Rodrigues rotation, utils.py:11-49); differentiable in torch."""
+    B = camPositions.shape[0]
+    x, y, z, w = camQuaternion.split(1, dim=-1)
+    x2, y2, z2, w2 = x * x, y * y, z * z, w * w
+    xy, zw, xz, yw, yz, xw = x * y, z * w, x * z, y * w, y * z, x * w
+    row0 = th.cat([x2 - y2 - z2 + w2, 2 * (xy - zw), 2 * (xz + yw)], dim=-1)
+    row1 = th.cat([2 * (xy + zw), -x2 + y2 - z2 + w2, 2 * (yz - xw)], dim=-1)
+    row2 = th.cat([2 * (xz - yw), 2 * (yz + xw), -x2 - y2 + z2 + w2], dim=-1)
+    R = th.stack([row0, row1, row2], dim=-2)  # (B,3,3)
+    top = th.cat([R, camPositions.reshape(B, 3, 1)], dim=-1)
+    bottom = th.zeros((B, 1, 4), dtype=camPositions.dtype, device=camPositions.device)
+    bottom[..., 3] = 1.0
+    return th.cat([top, bottom], dim=-2).unsqueeze(1)
+
+
+def transformForward(viewMatrix: th.Tensor, forward: str) -> th.Tensor:
+    """utils.py:51-60: for forward == 'z' flip y and mirror z."""
+    if forward == "z":
+        flip = th.diag(th.tensor([1.0, -1.0, -1.0, 1.0], dtype=viewMatrix.dtype, device=viewMatrix.device))
+        viewMatrix = flip.view(1, 1, 4, 4) @ viewMatrix
+    return viewMatrix
+
+
+def conditionalNormalization(dx: th.Tensor, radius=1.0, eps=1e-4) -> th.Tensor:
+    """utils.py:147-150: scale rows with norm > 1 down to norm ~1."""
+    norm = dx.norm(dim=-1, keepdim=True)
+    scale = th.clamp(norm + eps, 1.0)
+    return dx.div(scale)
+
+
+# --------------------------------------------------------------- sampling
+class FmmSampling:
+    """extensions/__init__.py:106-117"""
+
+    @th.no_grad()
+    def __call__(self, width: int, height: int, focallength: float, points: th.Tensor, normals: th.Tensor,
+                 colors: th.Tensor, stdDevs: th.Tensor, numSamples: int, smoothing: float,
+                 precision: float = 0.001, **kwargs) -> th.Tensor:
+        return sampling.sample(width, height, focallength, points, normals, colors, stdDevs, numSamples, smoothing,
+                               precision, **kwargs)
+
+
+# --------------------------------------------------------------- transform
+class AffineTransform(th.autograd.Function):
+    @staticmethod
+    def forward(ctx, transformMatrix, vector):
+        ctx.save_for_backward(transformMatrix, vector)
+        return transform.affineForward(transformMatrix.contiguous(), vector.contiguous())
+
+    @staticmethod
+    def backward(ctx, gradIn):
+        M, v = ctx.saved_tensors
+        gM, gv = transform.affineBackward(gradIn.contiguous(), M.contiguous(), v.contiguous())
+        return gM, gv
+
+
+class LinearTransform(th.autograd.Function):
+    @staticmethod
+    def forward(ctx, transformMatrix, vector):
+        ctx.save_for_backward(transformMatrix, vector)
+        return transform.linearForward(transformMatrix.contiguous(), vector.contiguous())
+
+    @staticmethod
+    def backward(ctx, gradIn):
+        M, v = ctx.saved_tensors
+        gM, gv = transform.linearBackward(gradIn.contiguous(), M.contiguous(), v.contiguous())
+        return gM, gv
+
+
+# ------------------------------------------------------------------- EWA
+class EWASplatting(th.autograd.Function):
+    @staticmethod
+    def forward(ctx, width: int, height: int, focallength: float, indices: th.Tensor, points: th.Tensor,
+                normals: th.Tensor, stdDevs: th.Tensor, smoothing: float) -> th.Tensor:
+        points, normals, stdDevs = points.contiguous(), normals.contiguous(), stdDevs.contiguous()
+        weights = splatting.forward(width, height, focallength, indices, points, normals, stdDevs, smoothing)
+        ctx.save_for_backward(indices, points, normals, stdDevs)
+        ctx.width, ctx.height, ctx.focallength, ctx.smoothing = width, height, focallength, smoothing
+        return weights
+
+    @staticmethod
+    def backward(ctx, gradWeights):
+        indices, points, normals, stdDevs = ctx.saved_tensors
+        gradPoints, gradNormals, gradStdDevs = splatting.backward(ctx.width, ctx.height, ctx.focallength,
+                                                                  gradWeights.contiguous(), indices, points, normals,
+                                                                  stdDevs, ctx.smoothing)
+        gradPoints = conditionalNormalization(gradPoints)
+        gradStdDevs = conditionalNormalization(gradStdDevs)
+        gradPoints = th.nan_to_num(gradPoints, nan=0.0, posinf=float("inf"), neginf=float("-inf"))
+        gradStdDevs = th.nan_to_num(gradStdDevs, nan=0.0, posinf=float("inf"), neginf=float("-inf"))
+        return None, None, None, None, gradPoints, None, gradStdDevs, None
+
+
+# ------------------------------------------------------------ compositing
+class DepthFiltering(th.autograd.Function):
+    @staticmethod
+    def forward(ctx, indices, weights, width: int, height: int, focallength: float, points, normals):
+        weights, points, normals = weights.contiguous(), points.contiguous(), normals.contiguous()
+        ctx.save_for_backward(indices, weights, points, normals)
+        ctx.width, ctx.height, ctx.focallength = width, height, focallength
+        return filtering.forward(indices, weights, width, height, focallength, points, normals)
+
+    @staticmethod
+    def backward(ctx, gradIn):
+        indices, weights, points, normals = ctx.saved_tensors
+        gradWeights = filtering.backward(indices, weights, gradIn.contiguous(), ctx.width, ctx.height,
+                                         ctx.focallength, points, normals)
+        return None, gradWeights, None, None, None, None, None
+
+
+# ---------------------------------------------------------- interpolation
+class LinearInterpolation(th.autograd.Function):
+    @staticmethod
+    def forward(ctx, indices, weights, values):
+        weights, values = weights.contiguous(), values.contiguous()
+        ctx.save_for_backward(indices, weights, values)
+        return interpolation.forward(indices, weights, values)
+
+    @staticmethod
+    def backward(ctx, gradIn):
+        indices, weights, values = ctx.saved_tensors
+        gradWeights, gradValues = interpolation.backward(gradIn.contiguous(), indices, weights, values)
+        return None, gradWeights, gradValues
+
+
+# ---------------------------------------------------------------- shading
+class DiffuseShading(th.autograd.Function):
+    @staticmethod
+    def forward(ctx, directions, intensites, normals, diffuse):
+        directions, intensites = directions.contiguous(), intensites.contiguous()
+        normals, diffuse = normals.contiguous(), diffuse.contiguous()
+        ctx.save_for_backward(directions, intensites, normals, diffuse)
+        return shading.forward(directions, intensites, normals, diffuse)
+
+    @staticmethod
+    def backward(ctx, gradIn):
+        directions, intensites, normals, diffuse = ctx.saved_tensors
+        return tuple(shading.backward(gradIn.contiguous(), directions, intensites, normals, diffuse))
+
+
+class SphericalHarmonicShading(th.autograd.Function):
+    @staticmethod
+    def forward(ctx, coefficients, normals, diffuse):
+        coefficients, normals, diffuse = coefficients.contiguous(), normals.contiguous(), diffuse.contiguous()
+        ctx.save_for_backward(coefficients, normals, diffuse)
+        return shading.forwardSh(coefficients, normals, diffuse)
+
+    @staticmethod
+    def backward(ctx, gradIn):
+        coefficients, normals, diffuse = ctx.saved_tensors
+        return tuple(shading.backwardSh(gradIn.contiguous(), coefficients, normals, diffuse))
+
+
+__all__ = ["FmmSampling", "AffineTransform", "LinearTransform", "EWASplatting", "DepthFiltering",
+           "LinearInterpolation", "DiffuseShading", "SphericalHarmonicShading", "world2Camera", "transformForward",
+           "conditionalNormalization", "normalize", "dot"]

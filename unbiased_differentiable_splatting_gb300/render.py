@@ -1,0 +1,185 @@
+"""Renderer module with the interface of the reference's ``splatting/render.py``
+(``Splatting``, render.py:230-376) and the per-splat shading modules of
+``splatting/shading.py``.
+
+``Splatting.forward`` runs: world->camera transform of points and normals,
+back-face orientation, FMM sampling of K splats per pixel, EWA weights, depth
+compositing, shading / attribute interpolation.  Every stage is a CUDA op of
+libuds.so behind the autograd wrappers of ``extensions``.
+
+Difference from the reference: ``self.indices`` (render.py:296 copies the
+indices to the host on every forward) is a lazy property here, so a forward
+pass never synchronises with the host.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import torch as th
+
+from .extensions import (AffineTransform, DepthFiltering, DiffuseShading, EWASplatting, FmmSampling,
+                         LinearInterpolation, LinearTransform, SphericalHarmonicShading, dot, normalize,
+                         transformForward, world2Camera)
+
+
+@dataclass
+class RenderOptions:
+    """The argparse fields Splatting reads (optimization_geometry.py:60-121)."""
+
+    forward: str = "-z"
+    numSamples: int = 40
+    precision: float = 0.01
+    shadingMode: str = "forward"
+    dtype: str = "float"
+    device: str = "cuda:0"
+
+
+def _cosine(normal: th.Tensor, light: th.Tensor) -> th.Tensor:
+    return th.clamp(th.sum(light.mul(normal), dim=-1, keepdim=True), 0.0, 1.0)
+
+
+class BackfaceCulling(th.nn.Module):
+    """render.py:193-205: flip normals that face away from the camera."""
+
+    def forward(self, normals, camNormals):
+        facing = camNormals[..., 2].unsqueeze(-1) > 0
+        return th.where(facing, -normals, normals), th.where(facing, -camNormals, camNormals)
+
+
+class Lambert(th.nn.Module):
+    """shading.py:12-29: per-splat ambient + Lambert shading."""
+
+    def forward(self, ambientLight, lampDirections, lampIntensities, normals, diffuse):
+        bn, l, _ = lampDirections.shape
+        lampDirections = lampDirections.view(bn, l, 1, 3)
+        normals = normals.unsqueeze(1)
+        ambientIrradiance = ambientLight * diffuse
+        radiance = lampIntensities.view(lampIntensities.shape[0], l, 1, 3)
+        irradiance = radiance.mul(_cosine(normals, lampDirections))
+        brdf = diffuse.unsqueeze(1) / math.pi
+        return ambientIrradiance + th.mul(irradiance, brdf).sum(dim=1)
+
+
+def _sh_matrix(coefficients: th.Tensor) -> th.Tensor:
+    c1, c2, c3, c4, c5 = 0.429043, 0.511664, 0.743125, 0.886227, 0.247708
+    c = coefficients
+    M = th.stack([
+        th.stack([c1 * c[..., 8], c1 * c[..., 4], c1 * c[..., 7], c2 * c[..., 3]], -1),
+        th.stack([c1 * c[..., 4], -c1 * c[..., 8], c1 * c[..., 5], c2 * c[..., 1]], -1),
+        th.stack([c1 * c[..., 7], c1 * c[..., 5], c3 * c[..., 6], c2 * c[..., 2]], -1),
+        th.stack([c2 * c[..., 3], c2 * c[..., 1], c2 * c[..., 2], c4 * c[..., 0] - c5 * c[..., 6]], -1),
+    ], -1)
+    return M  # symmetric; column j is the j-th stacked vector
+
+
+class ForwardSphericalHaromic(th.nn.Module):
+    """shading.py:79-129: per-splat order-2 SH irradiance."""
+
+    def __init__(self) -> None:
+        super().__init__()
+        self.coefficients = th.nn.Parameter(th.empty(1, 3, 9))
+        with th.no_grad():
+            self.coefficients.uniform_(-0.1, 0.1)
+            self.coefficients[..., 0] = 0.5
+
+    def forward(self, normals, diffuse):
+        M = _sh_matrix(self.coefficients).view(1, 1, 3, 4, 4)
+        n = th.cat([normals, th.ones_like(normals[..., :1])], dim=-1).view(normals.shape[0], normals.shape[1], 1, 1, 4)
+        image = dot(n @ M, n, False)
+        return diffuse * image.squeeze(-1) / math.pi
+
+
+class DeferredSphericalHaromic(th.nn.Module):
+    """shading.py:61-76: per-pixel SH shading through the CUDA op."""
+
+    def __init__(self, batched=1) -> None:
+        super().__init__()
+        self.coefficients = th.nn.Parameter(th.empty(batched, 3, 9))
+        with th.no_grad():
+            self.coefficients.uniform_(-0.1, 0.1)
+            self.coefficients[..., 0] = 0.5
+
+    def forward(self, normals, diffuse):
+        return SphericalHarmonicShading.apply(self.coefficients, normals, diffuse)
+
+
+def _normalizeNormals(normals: th.Tensor) -> th.Tensor:
+    norms = normals.norm(dim=-1, keepdim=True)
+    normals = th.where(norms < 0.01, th.ones_like(normals), normals)
+    return normalize(normals)
+
+
+class Splatting(th.nn.Module):
+    """render.py:230-376.  ``opts`` needs ``forward``, ``numSamples``,
+    ``precision``, ``shadingMode`` (a RenderOptions or the reference's argparse
+    namespace); ``sample_kwargs`` are passed to the sampler (``seed``,
+    ``uniforms``, ``h``)."""
+
+    def __init__(self, opts, logger, width: int, height: int, focallength: float, zmin: float, zmax: float,
+                 smoothing: float) -> None:
+        super().__init__()
+        self.logger = logger
+        self.width, self.height, self.focallength = int(width), int(height), float(focallength)
+        self.coordForward = getattr(opts, "forward", "-z")
+        self.smoothing = float(smoothing)
+        self.numSamples = int(opts.numSamples)
+        self.precision = float(opts.precision)
+        self.shadingMode = opts.shadingMode
+        self.affineTransform = AffineTransform.apply
+        self.linearTransform = LinearTransform.apply
+        self.backface = BackfaceCulling()
+        self.sampling = FmmSampling()
+        self.ewa = EWASplatting.apply
+        self.depthBlending = DepthFiltering.apply
+        self.linearInterpolation = LinearInterpolation.apply
+        self.deferredShading = DiffuseShading.apply
+        self.forwardShading = Lambert()
+        self.sphericalHarmonics = DeferredSphericalHaromic()
+        self.forwardHarmonics = ForwardSphericalHaromic()
+        self.sample_kwargs = {}
+        self._indices = None
+
+    @property
+    def indices(self):
+        return None if self._indices is None else self._indices.cpu().clone()
+
+    def forward(self, camPositions, camOrientations, pointPositions, pointNormals, pointStdDevs, pointDiffuse,
+                ambientLight, lampDirections, lampIntensities, alpha=None):
+        transformMatrix = world2Camera(camPositions, camOrientations)
+        transformMatrix = transformForward(transformMatrix, self.coordForward).squeeze(1).contiguous()
+        camPoints = self.affineTransform(transformMatrix, pointPositions)
+        camNormals = self.linearTransform(transformMatrix, pointNormals)
+        pointNormals, backfaceNormals = self.backface(pointNormals, camNormals)
+        with th.no_grad():
+            indices = self.sampling(self.width, self.height, self.focallength, camPoints.detach(),
+                                    backfaceNormals.detach().contiguous(), pointDiffuse, pointStdDevs.detach(),
+                                    self.numSamples, self.smoothing, self.precision, **self.sample_kwargs)
+        self._indices = indices
+        ewaWeights = self.ewa(self.width, self.height, self.focallength, indices, camPoints, camNormals, pointStdDevs,
+                              self.smoothing)
+        depthWeights = self.depthBlending(indices, ewaWeights, self.width, self.height, self.focallength, camPoints,
+                                          camNormals)
+        camLampDirections = self.linearTransform(transformMatrix, lampDirections)
+        if self.shadingMode == "deferred":
+            ewaNormals = _normalizeNormals(self.linearInterpolation(indices, depthWeights, camNormals))
+            ewaDiffuse = self.linearInterpolation(indices, depthWeights, pointDiffuse)
+            image = self.deferredShading(camLampDirections, lampIntensities, ewaNormals.contiguous(), ewaDiffuse)
+        elif self.shadingMode == "forward":
+            shadedPoints = self.forwardShading(ambientLight, camLampDirections, lampIntensities, camNormals,
+                                               pointDiffuse)
+            image = self.linearInterpolation(indices, depthWeights, shadedPoints)
+        elif self.shadingMode == "sphericalHarmonics":
+            ewaNormals = self.linearInterpolation(indices, depthWeights, pointNormals)
+            ewaDiffuse = self.linearInterpolation(indices, depthWeights, pointDiffuse)
+            image = self.sphericalHarmonics(ewaNormals, ewaDiffuse)
+        elif self.shadingMode == "forwardHarmonics":
+            shadedPoints = self.forwardHarmonics(pointNormals, pointDiffuse)
+            image = self.linearInterpolation(indices, depthWeights, shadedPoints)
+        elif self.shadingMode == "None":
+            image = self.linearInterpolation(indices, depthWeights, pointDiffuse)
+        elif self.shadingMode == "silhouette":
+            image = th.clamp(th.sum(ewaWeights, dim=-1, keepdim=True), 0, 1)
+        else:
+            raise ValueError("Unkown shading mode")
+        return image, indices, depthWeights
