@@ -1,0 +1,356 @@
+"""Benchmark of the Poisson-sampled EWA splatting path on GB300.
+
+One step = forward + backward of the renderer over one synthetic view:
+world->camera transform, FMM tree build + Poisson sampling of K splats per
+pixel, EWA weights, depth compositing, per-splat Lambert shading and
+interpolation, L2 image loss, and the backward pass to splat and pose
+gradients.  Metric: fwd+bwd Msamples/s (one sample = one (view, pixel, k)).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload harmonic500k|harmonic100k|sphere4k]
+
+* value : device-resident inputs, CUDA events around each step on the
+          launching stream, L2 flushed (256 MiB write) before every step;
+* e2e   : the same step through the public API with host buffers: pinned
+          host->device copies of every input and a device->host read of the
+          loss inside the timed region;
+* roofline: the dominant kernel (the per-pixel descent) timed alone with
+          CUDA events; algorithmic bytes = tree read once + indices written;
+* cpu_baseline: the CPU oracle (C, OpenMP) on a band of pixel rows.
+Multi-GPU (torchrun) runs independent replicas (the path has no exchange).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (generator kwargs, K, precision)
+    "harmonic500k": dict(scene="harmonic", n=500_000, sd_range=(0.003, 0.01), width=1024, K=8, precision=0.01),
+    "harmonic100k": dict(scene="harmonic", n=100_000, sd_range=(0.0045, 0.009), width=512, K=8, precision=0.01),
+    "sphere4k": dict(scene="sphere", n=4096, width=128, K=8, precision=0.01),
+}
+
+
+def make_scene(wl):
+    from unbiased_differentiable_splatting_gb300 import scenes
+    if wl["scene"] == "harmonic":
+        return scenes.harmonic_scene(n=wl["n"], sd_range=wl["sd_range"], width=wl["width"], seed=0)
+    return scenes.sphere_scene(n=wl["n"], width=wl["width"], seed=0)
+
+
+def workload_name(name, wl):
+    return f"{name}: {wl['n']} surfels, {wl['width']}x{wl['width']}, K={wl['K']}, adaptive Hermite degree <= 16, " \
+           f"precision {wl['precision']}, Lambert shading, 1 view"
+
+
+def dist_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def start(self):
+        def run():
+            q = "clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
+                "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
+                "clocks_event_reasons.sw_power_cap"
+            while not self._stop.is_set():
+                try:
+                    out = subprocess.run(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                         timeout=5).stdout.strip()
+                    if out:
+                        self.samples.append([x.strip() for x in out.split(",")])
+                except Exception:
+                    pass
+                self._stop.wait(0.2)
+        self._t = threading.Thread(target=run, daemon=True)
+        self._t.start()
+
+    def stop(self):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if len(s) > 3 + i and s[3 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def cpu_sample(wl, scene, target_s=12.0):
+    """The oracle (FP32 restatement of the reference, OpenMP) on a band of
+    pixel rows of the same workload: full tree build, descent of the band,
+    EWA / compositing / interpolation forward and backward of the band.
+    Returns (Msamples/s, threads, description)."""
+    import oracle
+    from unbiased_differentiable_splatting_gb300 import scenes as S
+    import torch
+    W = H = wl["width"]
+    K, prec, f = wl["K"], wl["precision"], scene["focal"]
+    pts, nrm = S.camera_space(scene)
+    nrm_b = torch.where(nrm[..., 2:] > 0, -nrm, nrm)
+    p = pts.numpy()[0]
+    nb = nrm_b.numpy()[0]
+    n = nrm.numpy()[0]
+    sd = scene["stddevs"].numpy()[0]
+    col = scene["colors"].numpy()
+
+    def run(rows):
+        t0 = time.perf_counter()
+        h = oracle.view_bandwidth(W, H, f, p, nb, sd, 0.0)
+        r = oracle.cull_radius(h, prec)
+        tree = oracle.Tree(W, H, f, p, h, r, prec)
+        x0 = (W - rows) // 2
+        idx = tree.sample(W, H, K, prec, seed=1, x0=x0, x1=x0 + rows)[None]
+        w = oracle.splat_forward(W, H, f, idx, p[None], n[None], sd[None], 0.0)
+        dw = oracle.filter_forward(idx, w, W, H, f, p[None], n[None])
+        img = oracle.interp_forward(idx, dw, col)
+        g = np.ones_like(img)
+        gw, _ = oracle.interp_backward(g, idx, dw, col)
+        gdw = oracle.filter_backward(idx, w, gw, W, H, f, p[None], n[None])
+        oracle.splat_backward(W, H, f, gdw, idx, p[None], n[None], sd[None], 0.0)
+        return time.perf_counter() - t0
+
+    t = run(2)
+    rows = int(max(2, min(W, 2 * target_s / max(t, 1e-3))))
+    t = run(rows)
+    rows2 = int(max(2, min(W, rows * target_s / max(t, 1e-3))))
+    if rows2 != rows:
+        rows = rows2
+        t = run(rows)
+    msps = rows * H * K / t / 1e6
+    return msps, oracle.num_threads(), f"{rows} of {W} pixel rows of the {W}x{H} view (full tree build), " \
+                                       f"{t:.1f} s"
+
+
+def reference_arm(args, wl, name):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    scene = make_scene(wl)
+    vals = []
+    desc = ""
+    threads = 1
+    for i in range(args.warmup + args.steps):
+        v, threads, desc = cpu_sample(wl, scene, target_s=min(10.0, 60.0 / max(args.steps, 1)))
+        if i >= args.warmup:
+            vals.append(v)
+    value = float(np.median(vals))
+    print(json.dumps({
+        "impl": "reference", "metric": "fwd+bwd Msamples/s", "value": value, "unit": "Msamples/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": workload_name(name, wl)},
+        "cpu_baseline": {"value": value, "unit": "Msamples/s", "cores": threads, "kind": "port",
+                         "sample": desc},
+        "e2e": {"value": value, "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="harmonic500k", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return reference_arm(args, wl, args.workload)
+
+    import torch
+    import torch.distributed as dist
+
+    rank, world, local = dist_info()
+    if world > 1:
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    import unbiased_differentiable_splatting_gb300 as uds
+    from unbiased_differentiable_splatting_gb300 import _lib
+    from unbiased_differentiable_splatting_gb300.cudaExtensions import sampling
+    from unbiased_differentiable_splatting_gb300.render import RenderOptions, Splatting
+    L = uds.load()
+
+    scene = make_scene(wl)
+    W = H = wl["width"]
+    K = wl["K"]
+    S = W * H * K
+    opts = RenderOptions(forward="-z", numSamples=K, precision=wl["precision"], shadingMode="forward")
+    renderer = Splatting(opts, None, W, H, scene["focal"], 0.1, 100.0, smoothing=0.0).to(dev)
+    renderer.sample_kwargs = {"seed": 1234}
+    keys = ["cam_positions", "cam_orientations", "points", "normals", "stddevs", "colors", "ambient",
+            "lamp_directions", "lamp_intensities"]
+    host = {k: scene[k].contiguous().pin_memory() for k in keys}
+    d = {k: host[k].to(dev) for k in keys}
+    target = torch.zeros((1, W, H, 3), device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def step(inp):
+        pos = inp["cam_positions"].requires_grad_(True)
+        quat = inp["cam_orientations"].requires_grad_(True)
+        pts = inp["points"].requires_grad_(True)
+        nrm = inp["normals"].requires_grad_(True)
+        sd = inp["stddevs"].requires_grad_(True)
+        col = inp["colors"].requires_grad_(True)
+        img, _, _ = renderer(pos, quat, pts, nrm, sd, col, inp["ambient"], inp["lamp_directions"],
+                             inp["lamp_intensities"])
+        loss = ((img - target) ** 2).sum()
+        loss.backward()
+        return loss
+
+    # target image: the scene with positions perturbed by N(0, 0.005)
+    with torch.no_grad():
+        pert = dict(d)
+        g = torch.Generator(device="cpu").manual_seed(1)
+        pert["points"] = (scene["points"] + 0.005 * torch.randn(scene["points"].shape, generator=g)).to(dev)
+        target, _, _ = renderer(pert["cam_positions"], pert["cam_orientations"], pert["points"], pert["normals"],
+                                pert["stddevs"], pert["colors"], pert["ambient"], pert["lamp_directions"],
+                                pert["lamp_intensities"])
+        target = target.detach()
+
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        step({k: v.detach().clone() for k, v in d.items()})
+    torch.cuda.synchronize(dev)
+
+    # ---- value: device-resident inputs
+    clocks = ClockSampler(local)
+    clocks.start()
+    times = []
+    launches0 = L.uds_launch_count()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    for _ in range(args.steps):
+        inp = {k: v.detach().clone() for k, v in d.items()}
+        flush.fill_(1)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step(inp)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize(dev)
+    launches = (L.uds_launch_count() - launches0) // max(args.steps, 1)
+    clk = clocks.stop()
+    t_step = float(np.sum(times)) / args.steps  # ms
+    if world > 1:
+        tt = torch.tensor([t_step], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_step = float(tt.item())
+    value = world * S / (t_step * 1e-3) / 1e6
+
+    # ---- e2e: host buffers, H2D of every input and D2H of the loss per step
+    h2d = sum(v.numel() * v.element_size() for v in host.values())
+    e2e_times = []
+    for _ in range(max(2, args.steps // 2)):
+        flush.fill_(1)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        inp = {k: v.to(dev, non_blocking=True) for k, v in host.items()}
+        loss = step(inp)
+        float(loss.item())
+        e2e_times.append(time.perf_counter() - t0)
+    t_e2e = float(np.median(e2e_times))
+    if world > 1:
+        tt = torch.tensor([t_e2e], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+    e2e = world * S / t_e2e / 1e6
+
+    # ---- roofline of the dominant kernel: the per-pixel descent alone
+    with torch.no_grad():
+        from unbiased_differentiable_splatting_gb300.extensions import transformForward, world2Camera
+        M = transformForward(world2Camera(d["cam_positions"], d["cam_orientations"]), "-z").squeeze(1).contiguous()
+        from unbiased_differentiable_splatting_gb300.cudaExtensions import transform
+        cp = transform.affineForward(M, d["points"])
+        cn = transform.linearForward(M, d["normals"])
+        cnb = torch.where(cn[..., 2:] > 0, -cn, cn).contiguous()
+        tree = sampling.build_tree(W, H, scene["focal"], cp, cnb, d["stddevs"], K, 0.0, wl["precision"])
+        prm = tree["_prm"]
+        prm.seed = 1234
+        ws = tree["_ws"]
+        idx = torch.full((W, H, K), -1, dtype=torch.int32, device=dev)
+        for _ in range(2):
+            _lib.check(L.uds_sample_descent(prm, 0, None, idx.data_ptr(), ws.data_ptr(), ws.numel(),
+                                            stream.cuda_stream), "descent")
+        dts = []
+        for _ in range(5):
+            flush.fill_(1)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            _lib.check(L.uds_sample_descent(prm, 0, None, idx.data_ptr(), ws.data_ptr(), ws.numel(),
+                                            stream.cuda_stream), "descent")
+            e1.record(stream)
+            e1.synchronize()
+            dts.append(e0.elapsed_time(e1))
+        t_desc = float(np.mean(dts)) * 1e-3
+        n = tree["n_visible"]
+        Mn = 2 * n - 1
+        bytes_alg = Mn * (16 + 4 + 16 + 16) + tree["n_coefs"] * 4 + n * (8 + 4) + W * H * K * 4
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        peak = json.load(open(peaks_path))["hbm_gbs"]
+        peak_src = "measured"
+    else:
+        peak, peak_src = 6800.0, "fallback"
+    achieved = bytes_alg / t_desc / 1e9
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        try:
+            v, thr, desc = cpu_sample(wl, scene)
+            cpu = {"value": v, "unit": "Msamples/s", "cores": thr, "kind": "port", "sample": desc}
+        except Exception as e:  # the CPU leg never decides the GPU result
+            cpu = {"value": None, "unit": "Msamples/s", "cores": 0, "kind": "port", "sample": f"failed: {e}"}
+
+    if rank == 0:
+        print(json.dumps({
+            "metric": "fwd+bwd Msamples/s", "value": value, "unit": "Msamples/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": workload_name(args.workload, wl), "l2": "flushed (256 MiB write) before each step",
+                       "parallelism": f"replicas x{world}"},
+            "e2e": {"value": e2e, "unit": "Msamples/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": 4},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None, "kernel": "k_sample (per-pixel descent)",
+                         "kernel_ms": t_desc * 1e3, "bytes_alg": int(bytes_alg), "peak_source": peak_src},
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "gpu_launches": int(launches),
+        }), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

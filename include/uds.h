@@ -40,6 +40,8 @@ const char* uds_status_string(int status);
 /* Last CUDA error text seen by a failing call on this host thread. */
 const char* uds_last_error(void);
 int uds_version(void);
+/* Number of kernels this library has enqueued since it was loaded. */
+unsigned long long uds_launch_count(void);
 
 /* Per-view record written by uds_sample (32 bytes). */
 typedef struct {
@@ -94,6 +96,12 @@ int uds_tree_build(const uds_sample_params* prm, int view, const float* points,
                    int32_t* right, int32_t* parent, int32_t* count, int32_t* degree,
                    float* centre, float* box, void* workspace, size_t workspace_bytes,
                    void* stream);
+/* The per-pixel descent alone (the last stage of uds_sample) on the tree of
+ * `view` already built in `workspace` by uds_tree_build; `indices` (W,H,K)
+ * for that view, not preset (pixels without samples are left untouched, so
+ * fill it with -1 first).  Used to time the dominant kernel on its own. */
+int uds_sample_descent(const uds_sample_params* prm, int view, const float* uniforms,
+                       int32_t* indices, void* workspace, size_t workspace_bytes, void* stream);
 /* FGT node masses (getWeight) of an already built tree (same workspace,
  * after uds_tree_build): m queries (node id, x, y) -> out[m]. */
 int uds_fgt_eval(const uds_sample_params* prm, int m, const int32_t* nodes, const float* query_xy,

@@ -303,6 +303,17 @@ class Tree:
         q = np.asarray(query, np.float64)
         return lib().orc_tree_direct_weight(ctypes.c_void_p(self.ptr), C(node), P(q))
 
+    def candidates(self, K, precision, i, j, flavour=None):
+        """(splat ids, leaf masses) of every candidate entry of pixel (i, j)."""
+        R = num_rounds(K)
+        ids = np.zeros(R * K, np.int32)
+        p = np.zeros(R * K, np.float32)
+        fl = self.flavour if flavour is None else flavour
+        m = lib().orc_tree_candidates(ctypes.c_void_p(self.ptr), C(K), F(precision), C(i), C(j), C(fl), P(ids), P(p))
+        if m < 0:
+            raise RuntimeError("oracle sampler trace overflow")
+        return ids[:m], p[:m]
+
     def sample(self, W, H, K, precision, uniforms=None, seed=0, view=0, x0=0, x1=None, flavour=None):
         idx = np.full((W, H, K), -1, np.int32)
         u = None if uniforms is None else _f(uniforms)

@@ -1235,6 +1235,58 @@ int orc_tree_sample(const orc_tree* t, int W, int H, int K, float precision, con
     return status;
 }
 
+/* Candidate entries of one pixel over all rounds: the descent is
+ * deterministic (masses and capacities do not depend on the uniforms), so the
+ * sampled indices are the K smallest keys u/p over these entries.  Writes
+ * splat ids and leaf masses p, returns the number of entries (<= R*K). */
+int orc_tree_candidates(const orc_tree* t, int K, float precision, int i, int j, int fl, int* ids,
+                        float* p) {
+    int R = orc_num_rounds(K);
+    int n = t->n, m = 0;
+    if (n == 0) return 0;
+    float q[2] = {(float)i, (float)j};
+    if (fmaxf(0.0f, orc_tree_node_weight(t, 0, q, fl)) < precision) return 0;
+    int tnode[8][ORC_STACK], tlen[8];
+    float tprob[8][ORC_STACK], tcap[8][ORC_STACK];
+    for (int r = 0; r < R && r < 8; ++r) {
+        int v = 0, d = 0;
+        tnode[r][0] = 0; tprob[r][0] = 1.0f;
+        while (t->count[v] > K) {
+            int a = t->left[v], b = t->right[v];
+            float w0 = fmaxf(0.0f, orc_tree_node_weight(t, a, q, fl));
+            float w1 = fmaxf(0.0f, orc_tree_node_weight(t, b, q, fl));
+            float sum = 0.0f;
+            sum += w0; sum += w1;
+            w0 = w0 / sum; w1 = w1 / sum;
+            float c0 = 1.0f, c1 = 1.0f;
+            for (int rr = r - 1; rr >= 0; --rr)
+                if (d + 1 < tlen[rr] && tnode[rr][d + 1] == a) { c0 = tcap[rr][d + 1]; break; }
+            for (int rr = r - 1; rr >= 0; --rr)
+                if (d + 1 < tlen[rr] && tnode[rr][d + 1] == b) { c1 = tcap[rr][d + 1]; break; }
+            ++d;
+            if (d >= ORC_STACK) return -1;
+            if (w0 * c0 < w1 * c1) { tnode[r][d] = b; tprob[r][d] = w1; v = b; }
+            else { tnode[r][d] = a; tprob[r][d] = w0; v = a; }
+        }
+        tlen[r] = d + 1;
+        float prob = 1.0f;
+        for (int mm = d; mm >= 0; --mm) {
+            float cap = 1.0f;
+            for (int rr = r - 1; rr >= 0; --rr)
+                if (mm < tlen[rr] && tnode[rr][mm] == tnode[r][mm]) { cap = tcap[rr][mm]; break; }
+            tcap[r][mm] = fmaxf(0.0f, cap - prob);
+            prob *= tprob[r][mm];
+        }
+        for (int k = 0; k < t->count[v]; ++k) {
+            int leafNode = n - 1 + t->first[v] + k;
+            ids[m] = t->ids[t->first[v] + k];
+            p[m] = fmaxf(0.0f, orc_tree_node_weight(t, leafNode, q, fl));
+            ++m;
+        }
+    }
+    return m;
+}
+
 int orc_sample_view(int W, int H, float f, int N, const float* pts, const float* nrm,
                     const float* sd, int K, float smoothing, float precision, float h_in,
                     const float* uniforms, uint64_t seed, uint32_t view, int flavour,

@@ -120,6 +120,11 @@ double orc_tree_direct_weight(const orc_tree* t, int node, const double* query);
 int orc_tree_sample(const orc_tree* t, int W, int H, int K, float precision, const float* uniforms,
                     uint64_t seed, uint32_t view, int x0, int x1, int flavour, int* indices);
 
+/* Candidate entries (splat id, leaf mass) of pixel (i, j) over all rounds;
+ * returns their number (<= ceil(sqrt(K)) * K). */
+int orc_tree_candidates(const orc_tree* t, int K, float precision, int i, int j, int flavour, int* ids,
+                        float* p);
+
 /* Whole-view convenience: h (if h <= 0), radius, build, sample.  Writes
  * stats[4] = {h, radius, n_visible, n_coefs}. */
 int orc_sample_view(int W, int H, float f, int N, const float* pts, const float* nrm,

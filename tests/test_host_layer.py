@@ -1,0 +1,83 @@
+"""Host-side logic that needs no GPU: input validation of the reference-named
+op modules, the view-matrix helpers, gradient post-processing, scenes."""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+
+def test_ops_reject_cpu_tensors():
+    from unbiased_differentiable_splatting_gb300.cudaExtensions import interpolation, sampling, splatting, transform
+    with pytest.raises(ValueError):
+        transform.affineForward(torch.eye(4)[None], torch.zeros(1, 3, 3))
+    with pytest.raises(ValueError):
+        sampling.sample(8, 8, 8.0, torch.zeros(1, 3, 3), torch.zeros(1, 3, 3), None, torch.zeros(1, 3, 2), 4, 0.0,
+                        0.01)
+    with pytest.raises((ValueError, TypeError)):
+        splatting.forward(8, 8, 8.0, torch.zeros(1, 8, 8, 4, dtype=torch.int32), torch.zeros(1, 3, 3),
+                          torch.zeros(1, 3, 3), torch.zeros(1, 3, 2), 0.0)
+    with pytest.raises((ValueError, TypeError)):
+        interpolation.forward(torch.zeros(1, 2, 2, 1), torch.zeros(1, 2, 2, 1), torch.zeros(1, 3, 3))
+
+
+def test_world2camera_matches_reference_formula():
+    from unbiased_differentiable_splatting_gb300.extensions import transformForward, world2Camera
+    rng = np.random.default_rng(0)
+    q = rng.normal(size=(5, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    t = rng.normal(size=(5, 3))
+    M = world2Camera(torch.tensor(t), torch.tensor(q)).numpy()
+    assert M.shape == (5, 1, 4, 4)
+    for b in range(5):
+        x, y, z, w = q[b]
+        R = np.array([[x * x - y * y - z * z + w * w, 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                      [2 * (x * y + z * w), -x * x + y * y - z * z + w * w, 2 * (y * z - x * w)],
+                      [2 * (x * z - y * w), 2 * (y * z + x * w), -x * x - y * y + z * z + w * w]])
+        np.testing.assert_allclose(M[b, 0, :3, :3], R, atol=1e-12)
+        np.testing.assert_allclose(M[b, 0, :3, 3], t[b])
+        np.testing.assert_allclose(M[b, 0, 3], [0, 0, 0, 1])
+        np.testing.assert_allclose(R @ R.T, np.eye(3), atol=1e-9)
+    Mz = transformForward(torch.tensor(M), "z").numpy()
+    np.testing.assert_allclose(Mz[:, 0, 1], -M[:, 0, 1])
+    np.testing.assert_allclose(Mz[:, 0, 2], -M[:, 0, 2])
+    np.testing.assert_allclose(Mz[:, 0, 0], M[:, 0, 0])
+
+
+def test_world2camera_is_differentiable():
+    from unbiased_differentiable_splatting_gb300.extensions import world2Camera
+    q = torch.tensor([[0.1, 0.2, 0.3, 0.9]], dtype=torch.float64, requires_grad=True)
+    t = torch.tensor([[0.0, 0.5, -2.0]], dtype=torch.float64, requires_grad=True)
+    assert torch.autograd.gradcheck(lambda a, b: world2Camera(a, b), (t, q))
+
+
+def test_conditional_normalization():
+    from unbiased_differentiable_splatting_gb300.extensions import conditionalNormalization
+    g = torch.tensor([[3.0, 4.0, 0.0], [0.1, 0.0, 0.0]])
+    out = conditionalNormalization(g)
+    assert math.isclose(float(out[0].norm()), 5.0 / 5.0001, rel_tol=1e-6)
+    assert torch.allclose(out[1], g[1])
+
+
+def test_scenes_are_seeded():
+    from unbiased_differentiable_splatting_gb300 import scenes
+    a = scenes.harmonic_scene(n=2000, width=64, seed=3)
+    b = scenes.harmonic_scene(n=2000, width=64, seed=3)
+    assert torch.equal(a["points"], b["points"]) and torch.equal(a["normals"], b["normals"])
+    n = a["normals"][0].numpy()
+    np.testing.assert_allclose(np.linalg.norm(n, axis=1), 1.0, atol=1e-5)
+    # outward normals
+    assert (np.sum(n * a["points"][0].numpy(), axis=1) > 0).mean() > 0.95
+    s = scenes.sphere_scene()
+    assert s["points"].shape == (1, 4096, 3) and abs(s["focal"] - 64 / math.tan(math.radians(30))) < 1e-9
+    pts, nrm = scenes.camera_space(s)
+    assert (pts[..., 2] < 0).all()
+
+
+def test_room_scene_cameras_look_at_walls():
+    from unbiased_differentiable_splatting_gb300 import scenes
+    sc = scenes.room_scene(n=20000, views=4, seed=1)
+    pts, _ = scenes.camera_space(sc)
+    assert sc["cam_positions"].shape == (4, 3)
+    # every view sees a good share of the room in front of it
+    assert ((pts[..., 2] < 0).float().mean(1) > 0.2).all()

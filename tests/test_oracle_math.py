@@ -1,0 +1,210 @@
+"""Properties of the CPU oracle itself: deterministic elementary functions,
+Philox uniforms, FGT accuracy against the FP64 direct Gauss sum, EWA
+gradients against central differences, agreement of the deterministic and
+the libm arithmetic, and the statistics of the Poisson order sampling."""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+
+
+def ulp_dist(a, b):
+    a = np.asarray(a, np.float32).view(np.int32).astype(np.int64)
+    b = np.asarray(b, np.float32).view(np.int32).astype(np.int64)
+    return np.abs(a - b)
+
+
+def test_det_expf_accuracy():
+    xs = np.concatenate([np.linspace(-87, 88, 20001), np.linspace(-1e-3, 1e-3, 101), [0.0, -20.5, -0.5]])
+    xs = xs.astype(np.float32)
+    got = np.array([oracle.det_expf(x) for x in xs], np.float32)
+    ref = np.exp(xs.astype(np.float64)).astype(np.float32)
+    assert ulp_dist(got, ref).max() <= 2
+    assert oracle.det_expf(-200.0) == 0.0
+    assert math.isinf(oracle.det_expf(100.0))
+    assert math.isnan(oracle.det_expf(float("nan")))
+
+
+def test_det_logf_accuracy():
+    xs = np.concatenate([np.geomspace(1e-30, 1e30, 20001), np.linspace(0.5, 2.0, 1001), [1e-40, 2.0 ** -140]])
+    xs = xs.astype(np.float32)
+    got = np.array([oracle.det_logf(x) for x in xs], np.float32)
+    ref = np.log(xs.astype(np.float64)).astype(np.float32)
+    close = np.abs(ref) > 1e-3
+    assert ulp_dist(got[close], ref[close]).max() <= 2
+    assert np.max(np.abs(got[~close] - ref[~close])) < 1e-9
+    assert oracle.det_logf(1.0) == 0.0
+    assert math.isinf(oracle.det_logf(0.0)) and math.isnan(oracle.det_logf(-1.0))
+
+
+def test_philox_uniforms():
+    u = np.array([oracle.philox_uniforms(99, 0, p, r, 8) for p in range(2000) for r in range(3)]).ravel()
+    assert u.min() > 0.0 and u.max() <= 1.0
+    # uniform on (0,1]: KS distance small
+    s = np.sort(u)
+    ks = np.max(np.abs(s - np.arange(1, len(s) + 1) / len(s)))
+    assert ks < 1.63 / math.sqrt(len(s)) * 1.2
+    np.testing.assert_array_equal(oracle.philox_uniforms(99, 0, 5, 1, 8), oracle.philox_uniforms(99, 0, 5, 1, 8))
+    assert not np.array_equal(oracle.philox_uniforms(99, 0, 5, 1, 8), oracle.philox_uniforms(98, 0, 5, 1, 8))
+    assert not np.array_equal(oracle.philox_uniforms(99, 0, 5, 1, 8), oracle.philox_uniforms(99, 1, 5, 1, 8))
+
+
+def _scene(rng, N, W, H, f, sd=(0.004, 0.012)):
+    z = rng.uniform(-2.4, -1.6, N)
+    pts = np.stack([rng.uniform(-0.5, 0.5, N) * (-z) * W / f, rng.uniform(-0.5, 0.5, N) * (-z) * H / f, z], 1)
+    n = rng.normal(size=(N, 3))
+    n[:, 2] = np.abs(n[:, 2]) + 0.5
+    n /= np.linalg.norm(n, axis=1, keepdims=True)
+    return pts.astype(np.float32), n.astype(np.float32), rng.uniform(sd[0], sd[1], size=(N, 2)).astype(np.float32)
+
+
+@pytest.mark.parametrize("precision", [0.01, 1e-4, 1e-6])
+def test_fgt_against_direct_sum(precision):
+    rng = np.random.default_rng(7)
+    W, H, f, N = 48, 48, 40.0, 3000
+    pts, nrm, sd = _scene(rng, N, W, H, f, sd=(0.01, 0.04))
+    h = oracle.view_bandwidth(W, H, f, pts, nrm, sd, 0.0)
+    t = oracle.Tree(W, H, f, pts, h, oracle.cull_radius(h, precision), precision)
+    e = t.export()
+    deg = e["degree"]
+    assert (deg[: t.n - 1] > 0).any(), "no Hermite expansions were built"
+    errs, rels = [], []
+    for _ in range(400):
+        v = int(rng.integers(0, 2 * t.n - 1))
+        q = rng.uniform(0, W, 2).astype(np.float32)
+        a = t.node_weight(v, q)
+        b = t.direct_weight(v, q.astype(np.float64))
+        errs.append(abs(a - b))
+        if b > 1e-2:
+            rels.append(abs(a - b) / b)
+    # absolute error bound: truncation (<= precision) + series (<= precision)
+    assert max(errs) <= 2 * precision + 1e-5
+    if precision <= 1e-4:
+        assert max(rels) < 1e-4  # "FGT node sums within 1e-4 relative of a direct FP64 Gauss sum"
+
+
+def test_ewa_gradient_finite_differences():
+    rng = np.random.default_rng(3)
+    W, H, f = 64.0, 64.0, 55.0
+    checked = 0
+    for _ in range(300):
+        p = np.array([rng.uniform(-0.3, 0.3), rng.uniform(-0.3, 0.3), rng.uniform(-2.3, -1.7)])
+        n = rng.normal(size=3)
+        n[2] = abs(n[2]) + 1.0
+        n /= np.linalg.norm(n)
+        sd = rng.uniform(0.01, 0.03, 2)
+        s = oracle.to_screenspace(W, H, f, p[None].astype(np.float32))[0]
+        pix = (np.round(s) + rng.integers(-1, 2, 2)).astype(np.float32)
+        _, raw = 0, np.zeros(1, np.float32)
+        w = oracle.lib().orc_ewa_weight(oracle.P(pix), oracle.F(W), oracle.F(H), oracle.F(f),
+                                        oracle.P(p.astype(np.float32)), oracle.P(n.astype(np.float32)),
+                                        oracle.P(sd.astype(np.float32)), oracle.F(0.0), oracle.P(raw))
+        if not (1e-3 < raw[0] < 1.0):
+            continue
+        gp, gn, gs = oracle.ewa_grad(pix, W, H, f, p, n, sd, 0.0)
+
+        def G(pp, nn, ss):
+            # FP64 forward of the same definition (the gradient's own forward)
+            s0 = -(pp[0] * f) / pp[2] + W / 2
+            s1 = (pp[1] * f) / pp[2] + H / 2
+
+            def bp(a, b):
+                return np.array([(W - 2 * a) / (2 * f), -(H - 2 * b) / (2 * f), 1.0])
+            x0, x1 = bp(s0 + 1, s1), bp(s0, s1 + 1)
+            c = pp @ nn
+            t0 = x0 * c / (x0 @ nn) - pp
+            t1 = x1 * c / (x1 @ nn) - pp
+            al = np.linalg.norm(t0)
+            u0 = t0 / al
+            be, ga = t1 @ u0, t1 @ np.cross(u0, nn)
+            J = np.linalg.inv(np.array([[al, be], [0, ga]]))
+            V = J @ np.diag(ss ** 2) @ J.T
+            d = pix - np.array([s0, s1])
+            return math.exp(-0.5 * d @ np.linalg.solve(V, d)) / (2 * math.pi * math.sqrt(np.linalg.det(V)) * abs(al * ga))
+        for vec, g, eps in ((p, gp, 1e-6), (n, gn, 1e-6), (sd, gs, 1e-8)):
+            fd = np.zeros_like(vec)
+            for k in range(len(vec)):
+                a = vec.copy(); a[k] += eps
+                b = vec.copy(); b[k] -= eps
+                args_a = [p, n, sd]; args_b = [p, n, sd]
+                idx = [id(p), id(n), id(sd)].index(id(vec))
+                args_a[idx] = a; args_b[idx] = b
+                fd[k] = (G(*args_a) - G(*args_b)) / (2 * eps)
+            assert np.linalg.norm(fd - g) <= 1e-5 * np.linalg.norm(fd) + 1e-9, (fd, g)
+        checked += 1
+    assert checked > 20
+
+
+def test_det_and_libm_sample_agree():
+    rng = np.random.default_rng(11)
+    W, H, f, N, K = 48, 48, 40.0, 2000, 8
+    pts, nrm, sd = _scene(rng, N, W, H, f)
+    a, sa = oracle.sample_view(W, H, f, pts, nrm, sd, K, 0.0, 0.01, seed=5)
+    b, sb = oracle.sample_view(W, H, f, pts, nrm, sd, K, 0.0, 0.01, seed=5, flavour=oracle.LIBM)
+    assert sa["n_visible"] == sb["n_visible"]
+    # the two differ only through last-ulp differences of exp / log / pow
+    assert (a != b).any(-1).mean() < 0.02
+
+
+def _inclusion_probabilities(p, K, grid=20000):
+    """Exact inclusion probability of each entry in the K smallest of
+    X_j = U_j / p_j, U_j ~ U(0,1] independent: integrate the density of X_j
+    against the Poisson-binomial law of the other keys below t."""
+    m = len(p)
+    if m <= K:
+        return np.where(p > 0, 1.0, 0.0)
+    out = np.zeros(m)
+    for j in range(m):
+        if p[j] <= 0:
+            continue
+        ts = (np.arange(grid) + 0.5) / grid / p[j]
+        others = np.delete(p, j)
+        q = np.minimum(1.0, np.outer(ts, others))  # P(X_i < t)
+        # P(count of others below t <= K-1) by dynamic programming
+        dist = np.zeros((grid, K))
+        dist[:, 0] = 1.0
+        for i in range(m - 1):
+            qi = q[:, i:i + 1]
+            new = dist * (1 - qi)
+            new[:, 1:] += dist[:, :-1] * qi
+            dist = new
+        out[j] = dist.sum(1).mean()  # density p_j over [0, 1/p_j]
+    return out
+
+
+def test_order_sampling_chi_square():
+    """Inclusion frequencies of the sampled splats against the exact order
+    sampling probabilities of the (deterministic) candidate entries."""
+    rng = np.random.default_rng(21)
+    W, H, f, N, K = 20, 20, 18.0, 700, 4
+    pts, nrm, sd = _scene(rng, N, W, H, f, sd=(0.02, 0.05))
+    h = oracle.view_bandwidth(W, H, f, pts, nrm, sd, 0.0)
+    t = oracle.Tree(W, H, f, pts, h, oracle.cull_radius(h, 0.01), 0.01)
+    pixels = []
+    for i in range(4, 16, 3):
+        for j in range(4, 16, 3):
+            ids, p = t.candidates(K, 0.01, i, j)
+            if len(ids) > K and len(np.unique(ids)) == len(ids) and (p > 0).sum() > K:
+                pixels.append((i, j, ids, p))
+    assert len(pixels) >= 4
+    runs = 3000
+    counts = {(i, j): np.zeros(len(ids)) for i, j, ids, _ in pixels}
+    for s in range(runs):
+        idx = t.sample(W, H, K, 0.01, seed=1000 + s)
+        for i, j, ids, _ in pixels:
+            got = set(idx[i, j].tolist())
+            counts[(i, j)] += np.array([1.0 if v in got else 0.0 for v in ids])
+    from scipy.stats import chi2
+    pvals = []
+    for i, j, ids, p in pixels:
+        P = _inclusion_probabilities(p.astype(np.float64), K)
+        E = runs * P
+        O = counts[(i, j)]
+        keep = (E >= 5) & (runs - E >= 5)
+        stat = np.sum((O[keep] - E[keep]) ** 2 / (E[keep] * (1 - P[keep])))
+        dof = max(int(keep.sum()) - 1, 1)
+        pvals.append(chi2.sf(stat, dof))
+    # Bonferroni over pixels at alpha = 1e-3
+    assert min(pvals) > 1e-3 / len(pvals), pvals

@@ -36,6 +36,7 @@ _SIGS = {
     "uds_status_string": (ctypes.c_char_p, [c_int]),
     "uds_last_error": (ctypes.c_char_p, []),
     "uds_version": (c_int, []),
+    "uds_launch_count": (ctypes.c_ulonglong, []),
     "uds_transform_forward": (c_int, [c_int, c_int, c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p]),
     "uds_transform_backward": (c_int, [c_int, c_int, c_void_p, c_void_p, c_int, c_int, c_void_p, c_void_p,
                                        c_void_p, c_void_p]),
@@ -45,6 +46,8 @@ _SIGS = {
     "uds_tree_build": (c_int, [ctypes.POINTER(SampleParams), c_int, c_void_p, c_void_p, c_void_p, c_void_p,
                                c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "uds_sample_descent": (c_int, [ctypes.POINTER(SampleParams), c_int, c_void_p, c_void_p, c_void_p, c_size_t,
+                                   c_void_p]),
     "uds_fgt_eval": (c_int, [ctypes.POINTER(SampleParams), c_int, c_void_p, c_void_p, c_void_p, c_void_p,
                              c_size_t, c_void_p]),
     "uds_splat_workspace_size": (c_size_t, [c_int, c_int]),

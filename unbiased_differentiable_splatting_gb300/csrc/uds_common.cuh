@@ -12,7 +12,7 @@ namespace uds {
 
 // ----------------------------------------------------------------- status
 void set_last_error(cudaError_t e);
-int launch_status();  // UDS_OK or UDS_ERR_LAUNCH after a kernel launch
+int launch_status(int launches = 1);  // UDS_OK or UDS_ERR_LAUNCH after `launches` kernel launches
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 

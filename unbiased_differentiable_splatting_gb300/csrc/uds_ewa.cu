@@ -46,7 +46,7 @@ __global__ void k_ewa_forward(int B, int W, int H, int K, const int* __restrict_
         size_t off = (size_t)s + (size_t)K * pix;
         int id = idx[off];
         float out = 0.0f;
-        if (id >= 0) {
+        if (id >= 0 && id < N) {
             size_t o = (size_t)id + (size_t)N * b;
             float4 a = consts[2 * o], c = consts[2 * o + 1];
             out = fminf(ewa_gauss(a, c, px, py), 1.0f);
@@ -69,7 +69,7 @@ __global__ void k_ewa_stats(int B, int W, int H, int K, const float* __restrict_
     for (int s = 0; s < K; ++s) {
         size_t off = (size_t)s + (size_t)K * pix;
         int id = idx[off];
-        if (id < 0) continue;
+        if (id < 0 || id >= N) continue;
         size_t o = (size_t)id + (size_t)N * b;
         float4 a = consts[2 * o], c = consts[2 * o + 1];
         float dx, dy;

@@ -21,8 +21,8 @@ __device__ __forceinline__ void pixel_ray(float W, float H, float f, float px, f
 }
 
 __device__ __forceinline__ float sample_depth(const float* dir, const float* __restrict__ pts,
-                                              const float* __restrict__ nrm, int id) {
-    if (id < 0) return kZmax;
+                                              const float* __restrict__ nrm, int id, int N) {
+    if (id < 0 || id >= N) return kZmax;
     float p[3] = {pts[3 * (size_t)id], pts[3 * (size_t)id + 1], pts[3 * (size_t)id + 2]};
     float n[3] = {nrm[3 * (size_t)id], nrm[3 * (size_t)id + 1], nrm[3 * (size_t)id + 2]};
     float d = fdiv(dot3(p, n), dot3(dir, n));
@@ -55,7 +55,7 @@ __global__ void k_filter_forward(int B, int W, int H, int K, const int* __restri
     pixel_ray((float)W, (float)H, f, (float)i, (float)j, dir);
     float dist[KMAX];
     int ord[KMAX];
-    for (int k = 0; k < K; ++k) dist[k] = sample_depth(dir, pts + po, nrm + po, idx[e + k]);
+    for (int k = 0; k < K; ++k) dist[k] = sample_depth(dir, pts + po, nrm + po, idx[e + k], N);
     depth_order<KMAX>(K, dist, ord);
     float rem = 1.0f;
     for (int q = 0; q < K; ++q) {
@@ -81,7 +81,7 @@ __global__ void k_filter_backward(int B, int W, int H, int K, const int* __restr
     float dist[KMAX], fw[KMAX], wl[KMAX];
     int ord[KMAX];
     for (int k = 0; k < K; ++k) {
-        dist[k] = sample_depth(dir, pts + po, nrm + po, idx[e + k]);
+        dist[k] = sample_depth(dir, pts + po, nrm + po, idx[e + k], N);
         wl[k] = w[e + k];
     }
     depth_order<KMAX>(K, dist, ord);

@@ -20,7 +20,7 @@ __global__ void k_interp_forward(int B, int W, int H, int K, const int* __restri
         for (int s = 0; s < K; ++s) {
             size_t so = (size_t)s + (size_t)K * pix;
             int id = idx[so];
-            if (id < 0) continue;
+            if (id < 0 || id >= N) continue;
             float wt = w[so];
             const float* a = attr + (size_t)C * ((size_t)id + (aB > 1 ? (size_t)N * b : 0)) + c0;
             for (int c = 0; c < cn; ++c) acc[c] = fadd(acc[c], fmul(wt, a[c]));
@@ -41,7 +41,7 @@ __global__ void k_interp_backward(int B, int W, int H, int K, const float* __res
     for (int s = 0; s < K; ++s) {
         size_t so = (size_t)s + (size_t)K * pix;
         int id = idx[so];
-        if (id < 0) { gw[so] = 0.0f; continue; }
+        if (id < 0 || id >= N) { gw[so] = 0.0f; continue; }
         float wt = w[so];
         size_t ao = (size_t)C * ((size_t)id + (aB > 1 ? (size_t)N * b : 0));
         float acc = 0.0f;

@@ -608,26 +608,34 @@ __device__ __forceinline__ bool truncated(const Tree& T, int v, float r, float q
     return !(d2 < fmul(r, r));
 }
 
-// getWeight / accumulateSubtree (evaluateDynamicRadixTree.cuh:129-242)
+// getWeight / accumulateSubtree (evaluateDynamicRadixTree.cuh:129-242):
+// stackless depth-first walk summing, in visiting order, the expansions of
+// the nodes that carry one and skipping subtrees whose box misses the
+// truncation circle.  A walk visits each node at most twice, so the step
+// budget 4n + 64 only guards against a malformed tree.
 __device__ float node_weight(const Tree& T, int v, float qx, float qy) {
     float4 c = T.cen[v];
     if (meta_degree(c.w) >= 0) return hermite_eval(T, v, c, qx, qy);
     int rootparent = T.par[v];
     float w = 0.0f;
+    int budget = 4 * T.n + 64;
     do {
         c = T.cen[v];
         while (meta_degree(c.w) < 0 && !truncated(T, v, c.z, qx, qy)) {
-            v = T.lnk[v].x;
+            int l = T.lnk[v].x;
+            if (l < 0 || --budget < 0) return w;
+            v = l;
             c = T.cen[v];
         }
         if (meta_degree(c.w) >= 0) w = fadd(w, hermite_eval(T, v, c, qx, qy));
         int p = T.par[v];
         while (p != rootparent && v == T.lnk[p].y) {
+            if (--budget < 0) return w;
             v = p;
             p = T.par[p];
         }
         if (p != rootparent) v = T.lnk[p].y;
-    } while (T.par[v] != rootparent);
+    } while (T.par[v] != rootparent && --budget >= 0);
     return w;
 }
 
@@ -769,7 +777,7 @@ static int build_view(const uds_sample_params* p, const Ws& w, int view, const f
         k_radix_hist<<<nb, kSortThreads, 0, s>>>(N, ki, shift, w.hist);
         k_radix_scan<<<1, 1024, 0, s>>>(w.hist, (int)(256 * nb));
         k_radix_scatter<<<nb, kSortThreads, 0, s>>>(N, ki, vi, ko, vo, shift, w.hist);
-        if ((st = launch_status())) return st;
+        if ((st = launch_status(3))) return st;
         uint32_t* t = ki; ki = ko; ko = t;
         t = vi; vi = vo; vo = t;
     }
@@ -779,7 +787,7 @@ static int build_view(const uds_sample_params* p, const Ws& w, int view, const f
     k_karras<<<nbN, 128, 0, s>>>(w.vs, ki, w.lnk, w.par);
     k_bottomup<<<nbN, 128, 0, s>>>(w.vs, p->precision, p->max_degree, w.lnk, w.par, w.box, w.cen, w.fanin);
     k_node_sizes<<<nbN, 128, 0, s>>>(w.vs, w.cen, w.sizes);
-    if ((st = launch_status())) return st;
+    if ((st = launch_status(4))) return st;
     unsigned sb = cdiv(N, kScanTile);
     k_scan_reduce<<<sb, kScanThreads, 0, s>>>(w.sizes, w.vs, 1, w.scanTmp);
     k_scan_top<<<1, 1024, 0, s>>>(w.scanTmp, (int)sb);
@@ -787,7 +795,7 @@ static int build_view(const uds_sample_params* p, const Ws& w, int view, const f
     k_assign<<<nbN, 128, 0, s>>>(w.vs, w.cen, w.sizes, w.offsets, w.coef_cap, w.stats + view);
     k_p2m<<<cdiv((size_t)N * 32, 128), 128, 0, s>>>(w.vs, w.lnk, w.cen, w.leaf_xy, w.coef);
     k_finish_view<<<1, 1, 0, s>>>(w.vs, w.stats + view);
-    return launch_status();
+    return launch_status(6);
 }
 
 static Tree tree_of(const Ws& w) {
@@ -923,6 +931,29 @@ extern "C" int uds_tree_build(const uds_sample_params* prm, int view, const floa
         if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
     }
     return UDS_OK;
+}
+
+extern "C" int uds_sample_descent(const uds_sample_params* prm, int view, const float* uniforms,
+                                  int32_t* indices, void* workspace, size_t workspace_bytes, void* stream) {
+    int st = check_params(prm);
+    if (st) return st;
+    if (view < 0 || view >= prm->B || !indices) return UDS_ERR_ARGUMENT;
+    Ws w = layout(prm, reinterpret_cast<char*>(workspace));
+    if (!workspace || workspace_bytes < w.bytes) return UDS_ERR_WORKSPACE;
+    if (prm->N == 0) return UDS_OK;
+    cudaStream_t s = as_stream(stream);
+    Tree T = tree_of(w);
+    switch (num_rounds(prm->K)) {
+        case 1: launch_sample<1>(T, w, prm, uniforms, view, indices, s); break;
+        case 2: launch_sample<2>(T, w, prm, uniforms, view, indices, s); break;
+        case 3: launch_sample<3>(T, w, prm, uniforms, view, indices, s); break;
+        case 4: launch_sample<4>(T, w, prm, uniforms, view, indices, s); break;
+        case 5: launch_sample<5>(T, w, prm, uniforms, view, indices, s); break;
+        case 6: launch_sample<6>(T, w, prm, uniforms, view, indices, s); break;
+        case 7: launch_sample<7>(T, w, prm, uniforms, view, indices, s); break;
+        default: launch_sample<8>(T, w, prm, uniforms, view, indices, s); break;
+    }
+    return launch_status();
 }
 
 extern "C" int uds_fgt_eval(const uds_sample_params* prm, int m, const int32_t* nodes, const float* query_xy,

@@ -17,7 +17,10 @@ void set_last_error(cudaError_t e) {
     g_last_error[k] = 0;
 }
 
-int launch_status() {
+unsigned long long g_launches = 0;  // kernels enqueued by this library
+
+int launch_status(int launches) {
+    __atomic_fetch_add(&g_launches, (unsigned long long)launches, __ATOMIC_RELAXED);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) return UDS_OK;
     set_last_error(e);
@@ -40,3 +43,5 @@ extern "C" const char* uds_status_string(int status) {
 extern "C" const char* uds_last_error(void) { return uds::g_last_error; }
 
 extern "C" int uds_version(void) { return 100; }
+
+extern "C" unsigned long long uds_launch_count(void) { return __atomic_load_n(&uds::g_launches, __ATOMIC_RELAXED); }

@@ -125,7 +125,6 @@ def build_tree(width, height, focallength, points, normals, stdDevs, numSamples,
     n = int(st["n_visible"][0])
     Mn = max(2 * n - 1, 0)
     res = {k: (v[:n] if k in ("keys", "ids") else v[:Mn]).cpu() for k, v in out.items()}
-    res["keys"] = res["keys"].view(torch.uint32) if hasattr(torch, "uint32") else res["keys"]
     res.update({k: float(v[0]) if k in ("h", "radius") else int(v[0]) for k, v in st.items()})
     res["_prm"] = prm
     res["_ws"] = ws
