@@ -149,7 +149,7 @@ def test_sample_sphere_128(smp):
     pts, nrm, sd, f, W = sphere_cam()
     got, st = _sample_both(smp, pts[None], nrm[None], sd[None], W, W, f, 8, seed=5)
     assert int(st["n_visible"][0]) == 4096
-    assert (got >= 0).mean() > 0.2
+    assert (got >= 0).mean() > 0.1
 
 
 def test_sample_edge_cases(smp):

@@ -640,11 +640,86 @@ __device__ float node_weight(const Tree& T, int v, float qx, float qy) {
 }
 
 // --------------------------------------------------------------- 8 sampler
+// Per-pixel mass cache.  getWeight(v) of a node without expansion that the
+// truncation circle reaches is the running sum, in depth-first order, of the
+// expansions below it; one walk from the root therefore yields getWeight of
+// every node it opens if each opened node keeps its own running sum, fed the
+// same values in the same order (so the sums are bit-identical to separate
+// walks).  The opened nodes are stored in pre-order with the index just past
+// their subtree, which locates both children of a cached node; the frontier
+// nodes whose expansion the walk evaluated are stored too.
+constexpr int kTable = 160;
+
+struct MassCache {
+    int node[kTable];
+    float mass[kTable];
+    int skip[kTable];
+    int m;
+    bool ok;
+};
+
+// getWeight(root); fills the cache (ok = false if it overflowed)
+__device__ float root_walk(const Tree& T, float qx, float qy, MassCache& mc) {
+    mc.m = 0;
+    mc.ok = true;
+    float4 c = T.cen[0];
+    if (meta_degree(c.w) >= 0) return hermite_eval(T, 0, c, qx, qy);
+    int stack[kTrace];
+    int sp = 0;
+    float total = 0.0f;
+    int v = 0;
+    int budget = 4 * T.n + 64;
+    do {
+        c = T.cen[v];
+        while (meta_degree(c.w) < 0 && !truncated(T, v, c.z, qx, qy)) {
+            if (mc.ok) {
+                if (mc.m < kTable && sp < kTrace) {
+                    mc.node[mc.m] = v;
+                    mc.mass[mc.m] = 0.0f;
+                    stack[sp++] = mc.m++;
+                } else {
+                    mc.ok = false;
+                }
+            }
+            int l = T.lnk[v].x;
+            if (l < 0 || --budget < 0) { mc.ok = false; return total; }
+            v = l;
+            c = T.cen[v];
+        }
+        if (meta_degree(c.w) >= 0) {
+            float val = hermite_eval(T, v, c, qx, qy);
+            total = fadd(total, val);
+            if (mc.ok) {
+                for (int s = 0; s < sp; ++s) mc.mass[stack[s]] = fadd(mc.mass[stack[s]], val);
+                // the frontier node itself: getWeight = its own expansion
+                if (mc.m < kTable) {
+                    mc.node[mc.m] = v;
+                    mc.mass[mc.m] = val;
+                    mc.skip[mc.m] = mc.m + 1;
+                    ++mc.m;
+                } else {
+                    mc.ok = false;
+                }
+            }
+        }
+        int p = T.par[v];
+        while (p != -1 && v == T.lnk[p].y) {
+            if (mc.ok) mc.skip[stack[--sp]] = mc.m;
+            if (--budget < 0) { mc.ok = false; return total; }
+            v = p;
+            p = T.par[p];
+        }
+        if (p != -1) v = T.lnk[p].y;
+    } while (T.par[v] != -1 && --budget >= 0);
+    return total;
+}
+
 template <int R, int KM>
 __global__ void __launch_bounds__(128) k_sample(Tree T, const ViewState* vs, int W, int H, int K,
                                                 float precision, const float* __restrict__ uniforms,
                                                 uint64_t seed, uint32_t view, int* __restrict__ indices,
                                                 uds_view_stats* st) {
+    // warp = 8 (y) x 4 (x) pixel tile: neighbouring pixels walk the same nodes
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     int i = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= W || j >= H) return;
@@ -654,7 +729,8 @@ __global__ void __launch_bounds__(128) k_sample(Tree T, const ViewState* vs, int
     int* out = indices + (size_t)K * pixel;
     if (T.n == 0) return;  // indices were preset to -1
     float qx = (float)i, qy = (float)j;
-    float total = fmaxf(0.0f, node_weight(T, 0, qx, qy));
+    MassCache mc;
+    float total = fmaxf(0.0f, root_walk(T, qx, qy, mc));
     if (total < precision) return;
     int ids[KM];
     float keys[KM];
@@ -663,6 +739,10 @@ __global__ void __launch_bounds__(128) k_sample(Tree T, const ViewState* vs, int
     float tc[R][kTrace];
     float tp[kTrace];
     int tl[R];
+    // child masses of the node met at each depth by the latest round
+    int cv[kTrace];
+    float cw0[kTrace], cw1[kTrace];
+    for (int d = 0; d < kTrace; ++d) cv[d] = -1;
     float u[KM];
     bool overflow = false;
     for (int r = 0; r < R; ++r) {
@@ -680,13 +760,29 @@ __global__ void __launch_bounds__(128) k_sample(Tree T, const ViewState* vs, int
             }
         }
         int v = 0, d = 0;
+        int e = (mc.ok && mc.m > 0) ? 0 : -1;  // cache entry of v
         tn[r][0] = 0;
         tp[0] = 1.0f;
         int4 L = T.lnk[0];
         while (L.w > K) {
             int a = L.x, b = L.y;
-            float w0 = fmaxf(0.0f, node_weight(T, a, qx, qy));
-            float w1 = fmaxf(0.0f, node_weight(T, b, qx, qy));
+            int ea = -1, eb = -1;
+            if (e >= 0) {
+                if (e + 1 < mc.m && mc.node[e + 1] == a) ea = e + 1;
+                int ib = ea >= 0 ? mc.skip[ea] : e + 1;
+                if (ib < mc.m && mc.node[ib] == b) eb = ib;
+            }
+            float w0, w1;
+            if (cv[d] == v) {
+                w0 = cw0[d];
+                w1 = cw1[d];
+            } else {
+                w0 = fmaxf(0.0f, ea >= 0 ? mc.mass[ea] : node_weight(T, a, qx, qy));
+                w1 = fmaxf(0.0f, eb >= 0 ? mc.mass[eb] : node_weight(T, b, qx, qy));
+                cv[d] = v;
+                cw0[d] = w0;
+                cw1[d] = w1;
+            }
             float sum = fadd(fadd(0.0f, w0), w1);
             w0 = fdiv(w0, sum);
             w1 = fdiv(w1, sum);
@@ -698,8 +794,8 @@ __global__ void __launch_bounds__(128) k_sample(Tree T, const ViewState* vs, int
             float s0 = fmul(w0, c0), s1 = fmul(w1, c1);
             ++d;
             if (d >= kTrace) { overflow = true; break; }
-            if (s0 < s1) { tn[r][d] = b; tp[d] = w1; v = b; }
-            else { tn[r][d] = a; tp[d] = w0; v = a; }
+            if (s0 < s1) { tn[r][d] = b; tp[d] = w1; v = b; e = eb; }
+            else { tn[r][d] = a; tp[d] = w0; v = a; e = ea; }
             L = T.lnk[v];
         }
         if (overflow) break;
@@ -713,11 +809,12 @@ __global__ void __launch_bounds__(128) k_sample(Tree T, const ViewState* vs, int
             prob = fmul(prob, tp[m]);
         }
         // order sampling over the subtree's leaves (insertSample,
-        // sequentialPoissonRadixTree.cuh:15-41)
+        // sequentialPoissonRadixTree.cuh:15-41); a leaf's mass is its own
+        // Gaussian (degree 0, coefficient 1)
         int f0 = L.z, cnt = L.w;
         for (int k = 0; k < cnt; ++k) {
             int leafNode = T.n - 1 + f0 + k;
-            float pw = fmaxf(0.0f, node_weight(T, leafNode, qx, qy));
+            float pw = fmaxf(0.0f, hermite_eval(T, leafNode, T.cen[leafNode], qx, qy));
             float key = fdiv(u[k], pw);
             int index = T.leaf_id[f0 + k];
             for (int q = 0; q < K; ++q) {
@@ -808,7 +905,7 @@ static Tree tree_of(const Ws& w) {
 template <int R>
 static void launch_sample(const Tree& T, const Ws& w, const uds_sample_params* p, const float* u, int view,
                           int* idx, cudaStream_t s) {
-    dim3 block(32, 4);
+    dim3 block(8, 16);
     dim3 grid(cdiv(p->H, block.x), cdiv(p->W, block.y));
     if (p->K <= 8)
         k_sample<R, 8><<<grid, block, 0, s>>>(T, w.vs, p->W, p->H, p->K, p->precision, u, p->seed, (uint32_t)view,
