@@ -122,6 +122,19 @@ int uds_splat_backward(int B, int W, int H, int K, float focal, const float* gra
                        float* grad_points, float* grad_normals, float* grad_std_devs,
                        void* workspace, size_t workspace_bytes, void* stream);
 
+/* splatting.forward without a workspace, for callers that cannot allocate
+ * device memory (a plugin slot that only passes the op's inputs and outputs,
+ * a language binding without a device allocator, a real-time loop that must
+ * not allocate after start-up).  No counterpart in the reference.  Same
+ * arguments and results as uds_splat_forward minus the workspace; the scratch
+ * is a fixed 8 MiB array inside the library, so B*N must not exceed 262144
+ * (larger calls return UDS_ERR_ARGUMENT).  The first call on a device looks
+ * the array up (make it before any stream capture); calls that overlap on the
+ * GPU share the array and race. */
+int uds_splat_forward_static(int B, int W, int H, int K, float focal, const int32_t* indices,
+                             const float* points, const float* normals, int std_batch, int N,
+                             const float* std_devs, float smoothing, float* weights, void* stream);
+
 /* ---- filtering.forward / backward (zSorting.cpp:24-43); points/normals
  *      (pB,N,3), pB = 1 or B. ---- */
 int uds_filter_forward(int B, int W, int H, int K, const int32_t* indices, const float* weights,

@@ -56,6 +56,8 @@ _SIGS = {
     "uds_splat_backward": (c_int, [c_int, c_int, c_int, c_int, c_float, c_void_p, c_void_p, c_void_p,
                                    c_void_p, c_int, c_int, c_void_p, c_float, c_void_p, c_void_p, c_void_p,
                                    c_void_p, c_size_t, c_void_p]),
+    "uds_splat_forward_static": (c_int, [c_int, c_int, c_int, c_int, c_float, c_void_p, c_void_p, c_void_p,
+                                         c_int, c_int, c_void_p, c_float, c_void_p, c_void_p]),
     "uds_filter_forward": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_float, c_int, c_int,
                                    c_void_p, c_void_p, c_void_p, c_void_p]),
     "uds_filter_backward": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_float, c_int,

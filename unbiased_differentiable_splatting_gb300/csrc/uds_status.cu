@@ -19,6 +19,12 @@ void set_last_error(cudaError_t e) {
 
 unsigned long long g_launches = 0;  // kernels enqueued by this library
 
+void set_last_error_message(const char* msg) {
+    int k = 0;
+    for (const char* p = msg; *p && k < 254; ++p) g_last_error[k++] = *p;
+    g_last_error[k] = 0;
+}
+
 int launch_status(int launches) {
     __atomic_fetch_add(&g_launches, (unsigned long long)launches, __ATOMIC_RELAXED);
     cudaError_t e = cudaGetLastError();
