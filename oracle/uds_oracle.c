@@ -1113,8 +1113,18 @@ static float hermite_eval(const orc_tree* t, int v, const float* q, int fl) {
     if (v >= t->n - 1) return 0.0f + (1.0f * hx[0]) * hy[0]; /* leaf: coefficient 1 */
     const float* C = &t->coef[t->offset[v]];
     float w = 0.0f;
-    for (int a = 0; a <= p; ++a)
-        for (int b = 0; b <= p; ++b) w += (C[a * (p + 1) + b] * hx[a]) * hy[b];
+    if (fl == ORC_LIBM) {
+        /* the reference's order: sum_a sum_b (C_ab h_a) h_b */
+        for (int a = 0; a <= p; ++a)
+            for (int b = 0; b <= p; ++b) w += (C[a * (p + 1) + b] * hx[a]) * hy[b];
+        return w;
+    }
+    /* row-factored with fused multiply-adds: sum_a h_a (sum_b C_ab h_b) */
+    for (int a = 0; a <= p; ++a) {
+        float s = 0.0f;
+        for (int b = 0; b <= p; ++b) s = fmaf(C[a * (p + 1) + b], hy[b], s);
+        w = fmaf(hx[a], s, w);
+    }
     return w;
 }
 

@@ -27,7 +27,8 @@ extern "C" {
 /* Arithmetic flavour of the sampler path.
  *  ORC_DET : the deterministic formulation the CUDA path computes
  *            (own exp/log from Cody-Waite reduction + Taylor polynomial,
- *            integer powers by repeated products; every other operation in
+ *            integer powers by repeated products, Hermite series summed
+ *            row-factored with fused multiply-adds; every other operation in
  *            the reference's order).  CUDA results must equal this bit for
  *            bit.
  *  ORC_LIBM: the reference's formulation (libm expf/logf/powf, unfused

@@ -568,7 +568,10 @@ struct Tree {
     float sq;
 };
 
-// evluateHermite with hermiteFunction (hermitefmm.cuh:35-47, 213-237)
+// evluateHermite with hermiteFunction (hermitefmm.cuh:35-47, 213-237): the
+// Hermite functions follow the reference's recursion; the series is summed
+// row-factored, sum_a h_a(tx) (sum_b C_ab h_b(ty)), with fused multiply-adds
+// (the CPU oracle's deterministic flavour sums the same way).
 __device__ __forceinline__ float hermite_eval(const Tree& T, int v, float4 c, float qx, float qy) {
     float tx = fdiv(fsub(qx, c.x), T.sq);
     float ty = fdiv(fsub(qy, c.y), T.sq);
@@ -591,9 +594,11 @@ __device__ __forceinline__ float hermite_eval(const Tree& T, int v, float4 c, fl
         if (a == 1) hx = fmul(tx2, ex);
         else if (a >= 2) hx = fsub(fmul(tx2, hxm1), fmul(fmul(2.0f, (float)(a - 1)), hxm2));
         const float* Ca = C + a * (p + 1);
+        float r = 0.0f;
 #pragma unroll
         for (int b = 0; b <= kMaxDegree; ++b)
-            if (b <= p) w = fadd(w, fmul(fmul(Ca[b], hx), hy[b]));
+            if (b <= p) r = __fmaf_rn(Ca[b], hy[b], r);
+        w = __fmaf_rn(hx, r, w);
         hxm2 = hxm1;
         hxm1 = hx;
     }
@@ -658,60 +663,108 @@ struct MassCache {
     bool ok;
 };
 
-// getWeight(root); fills the cache (ok = false if it overflowed)
-__device__ float root_walk(const Tree& T, float qx, float qy, MassCache& mc) {
+// Warp-cooperative walk.  The 32 pixels of a warp (an 8 x 4 tile) walk the
+// union of their trees in lock-step with an explicit stack of (node, lanes
+// inside, state) in shared memory.  At a node, every lane inside tests its
+// own truncation circle; lanes that open the node continue into its children,
+// the others leave that subtree.  Restricted to one lane, the union walk
+// visits exactly that lane's nodes in its own depth-first order, so the
+// running sums are unchanged; but expansion coefficients are now loaded once
+// per warp and the Hermite loops run with warp-uniform bounds.
+struct WalkStack {
+    int node[kTrace];
+    unsigned mask[kTrace];
+    int state[kTrace];  // 0 enter, 1 left subtree done, 2 both done
+};
+
+__device__ void warp_root_walk(const Tree& T, float qx, float qy, bool live, MassCache& mc, float& total,
+                               WalkStack& ws) {
+    const unsigned full = 0xffffffffu;
+    const int lane = (threadIdx.x + blockDim.x * threadIdx.y) & 31;
     mc.m = 0;
     mc.ok = true;
+    total = 0.0f;
+    unsigned liveMask = __ballot_sync(full, live);
     float4 c = T.cen[0];
-    if (meta_degree(c.w) >= 0) return hermite_eval(T, 0, c, qx, qy);
-    int stack[kTrace];
+    if (meta_degree(c.w) >= 0) {
+        if (live) total = hermite_eval(T, 0, c, qx, qy);
+        return;
+    }
+    if (!liveMask) return;
+    int ostack[kTrace];
+    int osp = 0;
     int sp = 0;
-    float total = 0.0f;
-    int v = 0;
-    int budget = 4 * T.n + 64;
-    do {
-        c = T.cen[v];
-        while (meta_degree(c.w) < 0 && !truncated(T, v, c.z, qx, qy)) {
-            if (mc.ok) {
-                if (mc.m < kTable && sp < kTrace) {
+    if (lane == 0) { ws.node[0] = 0; ws.mask[0] = liveMask; ws.state[0] = 0; }
+    __syncwarp();
+    int budget = 6 * T.n + 64;
+    while (sp >= 0) {
+        if (--budget < 0) { mc.ok = false; break; }
+        int v = ws.node[sp];
+        unsigned in = ws.mask[sp];
+        int stt = ws.state[sp];
+        bool mine = (in >> lane) & 1u;
+        __syncwarp();
+        if (stt == 0) {
+            c = T.cen[v];
+            if (meta_degree(c.w) >= 0) {
+                if (mine) {
+                    float val = hermite_eval(T, v, c, qx, qy);
+                    total = fadd(total, val);
+                    if (mc.ok) {
+                        for (int q = 0; q < osp; ++q) mc.mass[ostack[q]] = fadd(mc.mass[ostack[q]], val);
+                        if (mc.m < kTable) {
+                            mc.node[mc.m] = v;
+                            mc.mass[mc.m] = val;
+                            mc.skip[mc.m] = mc.m + 1;
+                            ++mc.m;
+                        } else {
+                            mc.ok = false;
+                        }
+                    }
+                }
+                --sp;
+                continue;
+            }
+            bool op = mine && !truncated(T, v, c.z, qx, qy);
+            unsigned opened = __ballot_sync(full, op);
+            if (!opened || sp + 1 >= kTrace) {
+                if (opened) mc.ok = false;  // deeper than any tree built here
+                --sp;
+                continue;
+            }
+            if (op && mc.ok) {
+                if (mc.m < kTable && osp < kTrace) {
                     mc.node[mc.m] = v;
                     mc.mass[mc.m] = 0.0f;
-                    stack[sp++] = mc.m++;
+                    ostack[osp++] = mc.m++;
                 } else {
                     mc.ok = false;
                 }
             }
             int l = T.lnk[v].x;
-            if (l < 0 || --budget < 0) { mc.ok = false; return total; }
-            v = l;
-            c = T.cen[v];
-        }
-        if (meta_degree(c.w) >= 0) {
-            float val = hermite_eval(T, v, c, qx, qy);
-            total = fadd(total, val);
-            if (mc.ok) {
-                for (int s = 0; s < sp; ++s) mc.mass[stack[s]] = fadd(mc.mass[stack[s]], val);
-                // the frontier node itself: getWeight = its own expansion
-                if (mc.m < kTable) {
-                    mc.node[mc.m] = v;
-                    mc.mass[mc.m] = val;
-                    mc.skip[mc.m] = mc.m + 1;
-                    ++mc.m;
-                } else {
-                    mc.ok = false;
-                }
+            if (lane == 0) {
+                ws.mask[sp] = opened;
+                ws.state[sp] = 1;
+                ws.node[sp + 1] = l;
+                ws.mask[sp + 1] = opened;
+                ws.state[sp + 1] = 0;
             }
+            ++sp;
+        } else if (stt == 1) {
+            int r = T.lnk[v].y;
+            if (lane == 0) {
+                ws.state[sp] = 2;
+                ws.node[sp + 1] = r;
+                ws.mask[sp + 1] = in;
+                ws.state[sp + 1] = 0;
+            }
+            ++sp;
+        } else {
+            if (mine && mc.ok) mc.skip[ostack[--osp]] = mc.m;
+            --sp;
         }
-        int p = T.par[v];
-        while (p != -1 && v == T.lnk[p].y) {
-            if (mc.ok) mc.skip[stack[--sp]] = mc.m;
-            if (--budget < 0) { mc.ok = false; return total; }
-            v = p;
-            p = T.par[p];
-        }
-        if (p != -1) v = T.lnk[p].y;
-    } while (T.par[v] != -1 && --budget >= 0);
-    return total;
+        __syncwarp();
+    }
 }
 
 template <int R, int KM>
@@ -719,44 +772,61 @@ __global__ void __launch_bounds__(128) k_sample(Tree T, const ViewState* vs, int
                                                 float precision, const float* __restrict__ uniforms,
                                                 uint64_t seed, uint32_t view, int* __restrict__ indices,
                                                 uds_view_stats* st) {
-    // warp = 8 (y) x 4 (x) pixel tile: neighbouring pixels walk the same nodes
+    // block 8 (y) x 16 (x); warp = 8 x 4 pixel tile
+    __shared__ WalkStack s_walk[4];
+    const unsigned full = 0xffffffffu;
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     int i = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= W || j >= H) return;
+    int tid = threadIdx.x + blockDim.x * threadIdx.y;
+    int warp = tid >> 5, lane = tid & 31;
+    bool live = (i < W && j < H);
     T.n = vs->n;
     T.sq = vs->sq;
+    if (T.n == 0) return;  // indices were preset to -1 (uniform over the grid)
     size_t pixel = (size_t)j + (size_t)H * i;
-    int* out = indices + (size_t)K * pixel;
-    if (T.n == 0) return;  // indices were preset to -1
     float qx = (float)i, qy = (float)j;
     MassCache mc;
-    float total = fmaxf(0.0f, root_walk(T, qx, qy, mc));
-    if (total < precision) return;
+    float total;
+    warp_root_walk(T, qx, qy, live, mc, total, s_walk[warp]);
+    total = fmaxf(0.0f, total);
+    bool act = live && !(total < precision);
+    if (!__any_sync(full, act)) return;
+    // K-sized arrays stay in registers for K <= 16 (loops fully unrolled)
+    constexpr int UK = KM <= 16 ? KM : 1;
     int ids[KM];
     float keys[KM];
-    for (int k = 0; k < K; ++k) { ids[k] = -1; keys[k] = __int_as_float(0x7f800000); }
+#pragma unroll UK
+    for (int k = 0; k < KM; ++k) { ids[k] = -1; keys[k] = __int_as_float(0x7f800000); }
     int tn[R][kTrace];
     float tc[R][kTrace];
     float tp[kTrace];
     int tl[R];
-    // child masses of the node met at each depth by the latest round
+    // child masses of the node met at each depth by the latest round; slots
+    // [0, cvn) are valid (depths are reached in order, so no clearing needed)
     int cv[kTrace];
     float cw0[kTrace], cw1[kTrace];
-    for (int d = 0; d < kTrace; ++d) cv[d] = -1;
+    int cvn = 0;
     float u[KM];
     bool overflow = false;
     for (int r = 0; r < R; ++r) {
-        if (uniforms) {
-            const float* up = uniforms + ((size_t)pixel * R + r) * K;
-            for (int k = 0; k < K; ++k) u[k] = up[k];
-        } else {
-            int G = (K + 3) >> 2;
-            for (int g = 0; g < G; ++g) {
-                uint32_t c4[4] = {(uint32_t)pixel, view, (uint32_t)(r * G + g), 0u};
-                philox4x32_10(c4, (uint32_t)seed, (uint32_t)(seed >> 32));
+        if (act) {
+            if (uniforms) {
+                const float* up = uniforms + ((size_t)pixel * R + r) * K;
+#pragma unroll UK
+                for (int k = 0; k < KM; ++k)
+                    if (k < K) u[k] = up[k];
+            } else {
+                int G = (K + 3) >> 2;
+#pragma unroll UK
+                for (int g = 0; g < (KM + 3) / 4; ++g) {
+                    if (g < G) {
+                        uint32_t c4[4] = {(uint32_t)pixel, view, (uint32_t)(r * G + g), 0u};
+                        philox4x32_10(c4, (uint32_t)seed, (uint32_t)(seed >> 32));
 #pragma unroll
-                for (int q = 0; q < 4; ++q)
-                    if (4 * g + q < K) u[4 * g + q] = bits_to_uniform(c4[q]);
+                        for (int q = 0; q < 4; ++q)
+                            if (4 * g + q < KM) u[4 * g + q] = bits_to_uniform(c4[q]);
+                    }
+                }
             }
         }
         int v = 0, d = 0;
@@ -764,41 +834,71 @@ __global__ void __launch_bounds__(128) k_sample(Tree T, const ViewState* vs, int
         tn[r][0] = 0;
         tp[0] = 1.0f;
         int4 L = T.lnk[0];
-        while (L.w > K) {
+        bool going = act && L.w > K;
+        while (__any_sync(full, going)) {
             int a = L.x, b = L.y;
+            float w0 = 0.0f, w1 = 0.0f;
             int ea = -1, eb = -1;
-            if (e >= 0) {
-                if (e + 1 < mc.m && mc.node[e + 1] == a) ea = e + 1;
-                int ib = ea >= 0 ? mc.skip[ea] : e + 1;
-                if (ib < mc.m && mc.node[ib] == b) eb = ib;
+            bool need = false;
+            if (going) {
+                if (e >= 0) {
+                    if (e + 1 < mc.m && mc.node[e + 1] == a) ea = e + 1;
+                    int ib = ea >= 0 ? mc.skip[ea] : e + 1;
+                    if (ib < mc.m && mc.node[ib] == b) eb = ib;
+                }
+                if (d < cvn && cv[d] == v) {
+                    w0 = cw0[d];
+                    w1 = cw1[d];
+                } else if (ea >= 0 && eb >= 0) {
+                    w0 = fmaxf(0.0f, mc.mass[ea]);
+                    w1 = fmaxf(0.0f, mc.mass[eb]);
+                } else {
+                    need = true;
+                }
             }
-            float w0, w1;
-            if (cv[d] == v) {
-                w0 = cw0[d];
-                w1 = cw1[d];
-            } else {
-                w0 = fmaxf(0.0f, ea >= 0 ? mc.mass[ea] : node_weight(T, a, qx, qy));
-                w1 = fmaxf(0.0f, eb >= 0 ? mc.mass[eb] : node_weight(T, b, qx, qy));
-                cv[d] = v;
-                cw0[d] = w0;
-                cw1[d] = w1;
+            // lanes at the same node evaluate its children's masses together
+            unsigned pend = __ballot_sync(full, need);
+            while (pend) {
+                int leader = __ffs(pend) - 1;
+                int vv = __shfl_sync(full, v, leader);
+                bool mineg = need && v == vv;
+                unsigned grp = __ballot_sync(full, mineg);
+                if (mineg) {
+                    w0 = fmaxf(0.0f, ea >= 0 ? mc.mass[ea] : node_weight(T, a, qx, qy));
+                    w1 = fmaxf(0.0f, eb >= 0 ? mc.mass[eb] : node_weight(T, b, qx, qy));
+                }
+                pend &= ~grp;
             }
-            float sum = fadd(fadd(0.0f, w0), w1);
-            w0 = fdiv(w0, sum);
-            w1 = fdiv(w1, sum);
-            float c0 = 1.0f, c1 = 1.0f;
-            for (int rr = r - 1; rr >= 0; --rr)
-                if (d + 1 < tl[rr] && tn[rr][d + 1] == a) { c0 = tc[rr][d + 1]; break; }
-            for (int rr = r - 1; rr >= 0; --rr)
-                if (d + 1 < tl[rr] && tn[rr][d + 1] == b) { c1 = tc[rr][d + 1]; break; }
-            float s0 = fmul(w0, c0), s1 = fmul(w1, c1);
-            ++d;
-            if (d >= kTrace) { overflow = true; break; }
-            if (s0 < s1) { tn[r][d] = b; tp[d] = w1; v = b; e = eb; }
-            else { tn[r][d] = a; tp[d] = w0; v = a; e = ea; }
-            L = T.lnk[v];
+            if (going) {
+                if (!(d < cvn && cv[d] == v)) {
+                    cv[d] = v;
+                    cw0[d] = w0;
+                    cw1[d] = w1;
+                    if (d >= cvn) cvn = d + 1;
+                }
+                float sum = fadd(fadd(0.0f, w0), w1);
+                w0 = fdiv(w0, sum);
+                w1 = fdiv(w1, sum);
+                float c0 = 1.0f, c1 = 1.0f;
+                for (int rr = r - 1; rr >= 0; --rr)
+                    if (d + 1 < tl[rr] && tn[rr][d + 1] == a) { c0 = tc[rr][d + 1]; break; }
+                for (int rr = r - 1; rr >= 0; --rr)
+                    if (d + 1 < tl[rr] && tn[rr][d + 1] == b) { c1 = tc[rr][d + 1]; break; }
+                float s0 = fmul(w0, c0), s1 = fmul(w1, c1);
+                ++d;
+                if (d >= kTrace) {
+                    overflow = true;
+                    going = false;
+                    act = false;
+                } else {
+                    if (s0 < s1) { tn[r][d] = b; tp[d] = w1; v = b; e = eb; }
+                    else { tn[r][d] = a; tp[d] = w0; v = a; e = ea; }
+                    L = T.lnk[v];
+                    going = L.w > K;
+                }
+            }
         }
-        if (overflow) break;
+        if (!act) continue;
         tl[r] = d + 1;
         float prob = 1.0f;
         for (int m = d; m >= 0; --m) {
@@ -812,22 +912,33 @@ __global__ void __launch_bounds__(128) k_sample(Tree T, const ViewState* vs, int
         // sequentialPoissonRadixTree.cuh:15-41); a leaf's mass is its own
         // Gaussian (degree 0, coefficient 1)
         int f0 = L.z, cnt = L.w;
-        for (int k = 0; k < cnt; ++k) {
-            int leafNode = T.n - 1 + f0 + k;
-            float pw = fmaxf(0.0f, hermite_eval(T, leafNode, T.cen[leafNode], qx, qy));
-            float key = fdiv(u[k], pw);
-            int index = T.leaf_id[f0 + k];
-            for (int q = 0; q < K; ++q) {
-                if (key < keys[q]) {
-                    int ti = ids[q]; ids[q] = index; index = ti;
-                    float tk = keys[q]; keys[q] = key; key = tk;
+#pragma unroll UK
+        for (int k = 0; k < KM; ++k) {
+            if (k < cnt) {
+                int leafNode = T.n - 1 + f0 + k;
+                float pw = fmaxf(0.0f, hermite_eval(T, leafNode, T.cen[leafNode], qx, qy));
+                float key = fdiv(u[k], pw);
+                int index = T.leaf_id[f0 + k];
+                bool done = false;
+#pragma unroll UK
+                for (int q = 0; q < KM; ++q) {
+                    if (!done && q < K) {
+                        if (key < keys[q]) {
+                            int ti = ids[q]; ids[q] = index; index = ti;
+                            float tk = keys[q]; keys[q] = key; key = tk;
+                        }
+                        if (index == -1) done = true;
+                    }
                 }
-                if (index == -1) break;
             }
         }
     }
     if (overflow) atomicAdd(&st->overflow, 1);
-    for (int k = 0; k < K; ++k) out[k] = ids[k];
+    if (!live) return;
+    int* out = indices + (size_t)K * pixel;
+#pragma unroll UK
+    for (int k = 0; k < KM; ++k)
+        if (k < K) out[k] = ids[k];
 }
 
 __global__ void k_finish_view(const ViewState* vs, uds_view_stats* st) {
@@ -907,12 +1018,12 @@ static void launch_sample(const Tree& T, const Ws& w, const uds_sample_params* p
                           int* idx, cudaStream_t s) {
     dim3 block(8, 16);
     dim3 grid(cdiv(p->H, block.x), cdiv(p->W, block.y));
-    if (p->K <= 8)
-        k_sample<R, 8><<<grid, block, 0, s>>>(T, w.vs, p->W, p->H, p->K, p->precision, u, p->seed, (uint32_t)view,
-                                              idx, w.stats + view);
+    if (R <= 3 && p->K <= 8)
+        k_sample<(R <= 3 ? R : 3), 8><<<grid, block, 0, s>>>(T, w.vs, p->W, p->H, p->K, p->precision, u, p->seed,
+                                                             (uint32_t)view, idx, w.stats + view);
     else
-        k_sample<R, kMaxK><<<grid, block, 0, s>>>(T, w.vs, p->W, p->H, p->K, p->precision, u, p->seed,
-                                                  (uint32_t)view, idx, w.stats + view);
+        k_sample<(R >= 3 ? R : 3), kMaxK><<<grid, block, 0, s>>>(T, w.vs, p->W, p->H, p->K, p->precision, u,
+                                                                 p->seed, (uint32_t)view, idx, w.stats + view);
 }
 
 static int check_params(const uds_sample_params* p) {
