@@ -101,9 +101,11 @@ class ClockSampler:
 
 
 def cpu_sample(wl, scene, target_s=12.0):
-    """The oracle (FP32 restatement of the reference, OpenMP) on a band of
-    pixel rows of the same workload: full tree build, descent of the band,
-    EWA / compositing / interpolation forward and backward of the band.
+    """The oracle (FP32 restatement of the reference, OpenMP over pixel rows)
+    on a bounded sample of the same workload: the full tree build of the view,
+    then descent + EWA / compositing / interpolation forward and backward on a
+    band of pixel rows sized to about `target_s` seconds.  The rate is scaled
+    to the whole image as S / (t_build + W * t_row).
     Returns (Msamples/s, threads, description)."""
     import oracle
     from unbiased_differentiable_splatting_gb300 import scenes as S
@@ -117,33 +119,46 @@ def cpu_sample(wl, scene, target_s=12.0):
     n = nrm.numpy()[0]
     sd = scene["stddevs"].numpy()[0]
     col = scene["colors"].numpy()
+    t0 = time.perf_counter()
+    h = oracle.view_bandwidth(W, H, f, p, nb, sd, 0.0)
+    r = oracle.cull_radius(h, prec)
+    tree = oracle.Tree(W, H, f, p, h, r, prec)
+    t_build = time.perf_counter() - t0
 
-    def run(rows):
+    def band(rows):
         t0 = time.perf_counter()
-        h = oracle.view_bandwidth(W, H, f, p, nb, sd, 0.0)
-        r = oracle.cull_radius(h, prec)
-        tree = oracle.Tree(W, H, f, p, h, r, prec)
         x0 = (W - rows) // 2
         idx = tree.sample(W, H, K, prec, seed=1, x0=x0, x1=x0 + rows)[None]
         w = oracle.splat_forward(W, H, f, idx, p[None], n[None], sd[None], 0.0)
         dw = oracle.filter_forward(idx, w, W, H, f, p[None], n[None])
         img = oracle.interp_forward(idx, dw, col)
-        g = np.ones_like(img)
-        gw, _ = oracle.interp_backward(g, idx, dw, col)
+        gw, _ = oracle.interp_backward(np.ones_like(img), idx, dw, col)
         gdw = oracle.filter_backward(idx, w, gw, W, H, f, p[None], n[None])
         oracle.splat_backward(W, H, f, gdw, idx, p[None], n[None], sd[None], 0.0)
         return time.perf_counter() - t0
 
-    t = run(2)
-    rows = int(max(2, min(W, 2 * target_s / max(t, 1e-3))))
-    t = run(rows)
-    rows2 = int(max(2, min(W, rows * target_s / max(t, 1e-3))))
-    if rows2 != rows:
-        rows = rows2
-        t = run(rows)
-    msps = rows * H * K / t / 1e6
-    return msps, oracle.num_threads(), f"{rows} of {W} pixel rows of the {W}x{H} view (full tree build), " \
-                                       f"{t:.1f} s"
+    t4 = band(4)
+    t_empty = band(0)  # the per-image passes over empty pixels
+    per_row = max((t4 - t_empty) / 4, 1e-6)
+    rows = int(max(4, min(W, (target_s - t_build - t_empty) / per_row)))
+    t = band(rows)
+    per_row = max((t - t_empty) / rows, 1e-9)
+    t_full = t_build + t_empty + W * per_row
+    msps = W * H * K / t_full / 1e6
+    return msps, oracle.num_threads(), (f"full tree build ({t_build:.1f} s) + {rows} of {W} pixel rows of the "
+                                        f"{W}x{H} view ({t:.1f} s), scaled to the whole view")
+
+
+def profiled_traffic(kernel="k_sample"):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "k_sample_k_p2m_harmonic500k_1024.md")
+    try:
+        for line in open(path):
+            if line.startswith(f"traffic_bytes_per_launch {kernel}:"):
+                return int(line.split(":")[1])
+    except OSError:
+        pass
+    return None
 
 
 def reference_arm(args, wl, name):
@@ -342,7 +357,9 @@ def main():
                        "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e, "unit": "Msamples/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": 4},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": None, "kernel": "k_sample (per-pixel descent)",
+                         "traffic": profiled_traffic() if args.workload == "harmonic500k" else None,
+                         "traffic_source": "ncu capture, profiles/k_sample_k_p2m_harmonic500k_1024.md",
+                         "kernel": "k_sample (per-pixel descent)",
                          "kernel_ms": t_desc * 1e3, "bytes_alg": int(bytes_alg), "peak_source": peak_src},
             "cpu_baseline": cpu,
             "clocks": clk,
