@@ -86,6 +86,18 @@ int uds_sample(const uds_sample_params* prm, const float* points, const float* n
                int32_t* indices, uds_view_stats* stats, void* workspace, size_t workspace_bytes,
                void* stream);
 
+/* Stochastic sampling mode (no counterpart in the reference, whose sampler is
+ * the deterministic Poisson descent above): each of the K draws of a pixel
+ * descends from the root into a child with probability proportional to its
+ * FGT mass and stops at a leaf.  indices (B,W,H,K) int32 as uds_sample;
+ * probs (B,W,H,K) float32 receives each draw's path probability q (the
+ * product of the ratios it took, ~ leaf mass / root mass), 0 where the draw
+ * is -1.  Uniforms are Philox4x32-10 keyed by prm->seed, counter
+ * (pixel, view, 2^31 | k<<8 | depth/4, 0).  Same workspace as uds_sample. */
+int uds_sample_stochastic(const uds_sample_params* prm, const float* points, const float* normals,
+                          const float* std_devs, const float* h_override, int32_t* indices, float* probs,
+                          uds_view_stats* stats, void* workspace, size_t workspace_bytes, void* stream);
+
 /* Debug view of one tree (for tests): builds view `view` and copies the
  * first n_visible entries of each array (host-sized by the caller from
  * stats).  Any output pointer may be NULL.  Arrays: keys/ids (n), node arrays

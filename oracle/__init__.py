@@ -303,6 +303,18 @@ class Tree:
         q = np.asarray(query, np.float64)
         return lib().orc_tree_direct_weight(ctypes.c_void_p(self.ptr), C(node), P(q))
 
+    def sample_stochastic(self, W, H, K, precision, seed=0, view=0, x0=0, x1=None, flavour=None):
+        """Stochastic mode: (indices (W,H,K), path probabilities (W,H,K))."""
+        idx = np.full((W, H, K), -1, np.int32)
+        prob = np.zeros((W, H, K), np.float32)
+        fl = self.flavour if flavour is None else flavour
+        st = lib().orc_tree_sample_stochastic(ctypes.c_void_p(self.ptr), C(W), C(H), C(K), F(precision),
+                                              ctypes.c_uint64(seed), ctypes.c_uint32(view), C(x0),
+                                              C(W if x1 is None else x1), C(fl), P(idx), P(prob))
+        if st != 0:
+            raise RuntimeError("oracle stochastic sampler: path deeper than 64 levels")
+        return idx, prob
+
     def candidates(self, K, precision, i, j, flavour=None):
         """(splat ids, leaf masses) of every candidate entry of pixel (i, j)."""
         R = num_rounds(K)
@@ -324,6 +336,14 @@ class Tree:
         if st != 0:
             raise RuntimeError("oracle sampler trace overflow")
         return idx
+
+
+def sample_view_stochastic(W, H, f, pts, nrm, sd, K, smoothing, precision, h=0.0, seed=0, view=0, flavour=DET):
+    """Stochastic sampling mode for one view: (indices (W,H,K), probs (W,H,K))."""
+    pts, nrm, sd = _f(pts).reshape(-1, 3), _f(nrm).reshape(-1, 3), _f(sd).reshape(-1, 2)
+    hh = h if h > 0 else view_bandwidth(W, H, f, pts, nrm, sd, smoothing)
+    t = Tree(W, H, f, pts, hh, cull_radius(hh, precision, flavour), precision, flavour=flavour)
+    return t.sample_stochastic(W, H, K, precision, seed=seed, view=view)
 
 
 def sample_view(W, H, f, pts, nrm, sd, K, smoothing, precision, h=0.0, uniforms=None, seed=0, view=0,

@@ -1245,6 +1245,60 @@ int orc_tree_sample(const orc_tree* t, int W, int H, int K, float precision, con
     return status;
 }
 
+/* Stochastic mode (no reference counterpart): each of the K draws of a
+ * pixel descends from the root, stepping into a child with probability
+ * m_child / (m_left + m_right) (masses by getWeight), until it reaches a
+ * leaf; the draw's path probability q is the product of the chosen ratios.
+ * Uniform for draw k at depth d: Philox counter (pixel, view,
+ * 2^31 | k << 8 | d / 4, 0), component d % 4; step left iff u <= ratio.
+ * A draw whose two child masses are both zero, or that is still above the
+ * leaves after 64 levels (the trace depth of the deterministic sampler), and
+ * every draw of a pixel whose root mass is below precision, give index -1 and
+ * q = 0. */
+int orc_tree_sample_stochastic(const orc_tree* t, int W, int H, int K, float precision, uint64_t seed,
+                               uint32_t view, int x0, int x1, int fl, int* indices, float* probs) {
+    int n = t->n;
+    int status = 0;
+    if (x1 > W) x1 = W;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int i = x0; i < x1; ++i) {
+        for (int j = 0; j < H; ++j) {
+            size_t pixel = (size_t)j + (size_t)H * i;
+            int* out = &indices[(size_t)K * pixel];
+            float* pq = &probs[(size_t)K * pixel];
+            for (int k = 0; k < K; ++k) { out[k] = -1; pq[k] = 0.0f; }
+            if (n == 0) continue;
+            float q[2] = {(float)i, (float)j};
+            if (fmaxf(0.0f, orc_tree_node_weight(t, 0, q, fl)) < precision) continue;
+            for (int k = 0; k < K; ++k) {
+                int v = 0, d = 0;
+                float prob = 1.0f;
+                uint32_t c[4];
+                int ok = 1;
+                while (v < n - 1) {
+                    if ((d & 3) == 0) {
+                        c[0] = (uint32_t)pixel; c[1] = view; c[2] = 0x80000000u | ((uint32_t)k << 8) | (uint32_t)(d >> 2); c[3] = 0;
+                        philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+                    }
+                    float u = (float)((c[d & 3] >> 8) + 1u) * 0x1p-24f;
+                    int a = t->left[v], b = t->right[v];
+                    float w0 = fmaxf(0.0f, orc_tree_node_weight(t, a, q, fl));
+                    float w1 = fmaxf(0.0f, orc_tree_node_weight(t, b, q, fl));
+                    float sum = 0.0f;
+                    sum += w0; sum += w1;
+                    if (!(sum > 0.0f)) { ok = 0; break; }
+                    float r0 = w0 / sum;
+                    if (u <= r0) { prob *= r0; v = a; }
+                    else { prob *= w1 / sum; v = b; }
+                    if (++d >= ORC_STACK && v < n - 1) { ok = 0; status = -1; break; }
+                }
+                if (ok) { out[k] = t->ids[v - (n - 1)]; pq[k] = prob; }
+            }
+        }
+    }
+    return status;
+}
+
 /* Candidate entries of one pixel over all rounds: the descent is
  * deterministic (masses and capacities do not depend on the uniforms), so the
  * sampled indices are the K smallest keys u/p over these entries.  Writes

@@ -121,6 +121,11 @@ double orc_tree_direct_weight(const orc_tree* t, int node, const double* query);
 int orc_tree_sample(const orc_tree* t, int W, int H, int K, float precision, const float* uniforms,
                     uint64_t seed, uint32_t view, int x0, int x1, int flavour, int* indices);
 
+/* Stochastic mode: K independent mass-proportional descents per pixel;
+ * indices (W*H*K) and path probabilities probs (W*H*K). */
+int orc_tree_sample_stochastic(const orc_tree* t, int W, int H, int K, float precision, uint64_t seed,
+                               uint32_t view, int x0, int x1, int flavour, int* indices, float* probs);
+
 /* Candidate entries (splat id, leaf mass) of pixel (i, j) over all rounds;
  * returns their number (<= ceil(sqrt(K)) * K). */
 int orc_tree_candidates(const orc_tree* t, int K, float precision, int i, int j, int flavour, int* ids,

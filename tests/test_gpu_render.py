@@ -1,0 +1,188 @@
+"""The Splatting renderer end to end on the GPU against the CPU oracle's
+pipeline, finite-difference checks of the GPU gradient chain, and CUDA-graph
+capture of the sampler.
+
+Image tolerance: 1e-5 relative L2 (the weights differ from the oracle only by
+CUDA's expf).  Finite differences: central, FP32 forward with fixed indices.
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda:0"
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+
+
+@pytest.fixture(scope="module")
+def uds():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import unbiased_differentiable_splatting_gb300 as u
+    u.load()
+    return u
+
+
+def _scene(n=3000, W=64, seed=0):
+    from unbiased_differentiable_splatting_gb300 import scenes
+    return scenes.harmonic_scene(n=n, sd_range=(0.01, 0.02), width=W, seed=seed)
+
+
+@pytest.mark.parametrize("mode", ["forward", "None"])
+def test_splatting_module_matches_oracle_pipeline(uds, mode):
+    from unbiased_differentiable_splatting_gb300.render import RenderOptions, Splatting
+    from unbiased_differentiable_splatting_gb300 import scenes
+    sc = _scene()
+    W = sc["width"]
+    f = sc["focal"]
+    K = 8
+    opts = RenderOptions(numSamples=K, precision=0.01, shadingMode=mode)
+    r = Splatting(opts, None, W, W, f, 0.1, 100.0, 0.0).to(DEV)
+    r.sample_kwargs = {"seed": 77}
+    d = {k: v.to(DEV) for k, v in sc.items() if isinstance(v, torch.Tensor)}
+    img, idx, dw = r(d["cam_positions"], d["cam_orientations"], d["points"], d["normals"], d["stddevs"], d["colors"],
+                     d["ambient"], d["lamp_directions"], d["lamp_intensities"])
+    torch.cuda.synchronize()
+    # oracle pipeline on the same camera-space inputs (the GPU transform is
+    # bit-exact with the oracle's)
+    M = torch.eye(4)[None]
+    M[0, 2, 3] = -2.0
+    P = oracle.transform_forward(M.numpy(), sc["points"].numpy(), True)
+    Nn = oracle.transform_forward(M.numpy(), sc["normals"].numpy(), False)
+    Nb = np.where(Nn[..., 2:] > 0, -Nn, Nn)
+    sd = sc["stddevs"].numpy()
+    idx_o, st = oracle.sample_view(W, W, f, P[0], Nb[0], sd[0], K, 0.0, 0.01, seed=77)
+    np.testing.assert_array_equal(idx.cpu().numpy()[0], idx_o)
+    w = oracle.splat_forward(W, W, f, idx_o[None], P, Nn, sd, 0.0)
+    dwo = oracle.filter_forward(idx_o[None], w, W, W, f, P, Nn)
+    assert rel_l2(dw.cpu().numpy(), dwo) < 1e-5
+    col = sc["colors"].numpy()
+    if mode == "forward":
+        ldir = oracle.transform_forward(M.numpy(), sc["lamp_directions"].numpy(), False)
+        cosv = np.clip(np.sum(Nn[0][None] * ldir[0][:, None], -1, keepdims=True), 0, 1)  # (L,N,1)
+        shaded = sc["ambient"].numpy() * col + np.sum(sc["lamp_intensities"].numpy()[0][:, None] * cosv *
+                                                      col[0][None] / np.pi, 0)
+        col = shaded.astype(np.float32)
+    img_o = oracle.interp_forward(idx_o[None], dwo, col)
+    assert rel_l2(img.detach().cpu().numpy(), img_o) < 1e-5
+    # backward runs and yields finite gradients for every differentiable input
+    for k in ("points", "stddevs", "colors", "cam_positions", "cam_orientations"):
+        d[k].requires_grad_(True)
+    img, _, _ = r(d["cam_positions"], d["cam_orientations"], d["points"], d["normals"], d["stddevs"], d["colors"],
+                  d["ambient"], d["lamp_directions"], d["lamp_intensities"])
+    (img ** 2).sum().backward()
+    for k in ("points", "stddevs", "colors", "cam_positions", "cam_orientations"):
+        g = d[k].grad
+        assert g is not None and torch.isfinite(g).all() and g.abs().sum() > 0, k
+
+
+def test_gradient_chain_finite_differences(uds):
+    """EWA -> compositing -> interpolation with fixed indices: the GPU
+    backward against central differences of the GPU forward.
+
+    The compositing backward follows the reference in dropping the terms whose
+    divisor w or 1 - w is within 1e-4 of zero (alphacompositingGrad.cuh:9-22),
+    and the EWA backward skips weights clamped at 1 (splattingCuda.cu:174);
+    the splats checked here have all their weights inside (1e-3, 1 - 1e-3),
+    where the gradient is the exact derivative.  Each pixel takes its K
+    nearest splats (screen distance), so most weights are well above 1e-3."""
+    from unbiased_differentiable_splatting_gb300.cudaExtensions import filtering, interpolation, splatting
+    rng = np.random.default_rng(3)
+    W = H = 24
+    f, K, N = 20.0, 4, 60
+    z = rng.uniform(-2.2, -1.8, N)
+    pts = np.stack([rng.uniform(-0.45, 0.45, N) * (-z) * W / f, rng.uniform(-0.45, 0.45, N) * (-z) * H / f, z], 1)
+    n = rng.normal(size=(N, 3))
+    n[:, 2] = np.abs(n[:, 2]) + 1.5
+    n /= np.linalg.norm(n, axis=1, keepdims=True)
+    sd = rng.uniform(0.4, 0.7, size=(1, N, 2))
+    col = rng.uniform(0.2, 1.0, size=(1, N, 3))
+    sx = -(pts[:, 0] * f) / pts[:, 2] + W / 2
+    sy = (pts[:, 1] * f) / pts[:, 2] + H / 2
+    gi, gj = np.meshgrid(np.arange(W), np.arange(H), indexing="ij")
+    dist = (gi[..., None] - sx) ** 2 + (gj[..., None] - sy) ** 2
+    idx = np.argsort(dist, axis=-1)[..., :K][None].astype(np.int32)
+    T = lambda a: torch.as_tensor(np.ascontiguousarray(a, np.float32)).to(DEV)  # noqa: E731
+    ti = torch.as_tensor(idx).to(DEV)
+    g_img = T(rng.normal(size=(1, W, H, 3)))
+
+    def loss(p, s):
+        w = splatting.forward(W, H, f, ti, p, T(n[None]), s, 0.0)
+        dw = filtering.forward(ti, w, W, H, f, p, T(n[None]))
+        img = interpolation.forward(ti, dw, T(col))
+        return float((img.double() * g_img.double()).sum())
+
+    p0, s0 = T(pts[None]), T(sd)
+    w = splatting.forward(W, H, f, ti, p0, T(n[None]), s0, 0.0)
+    dw = filtering.forward(ti, w, W, H, f, p0, T(n[None]))
+    gw, _ = interpolation.backward(g_img, ti, dw, T(col))
+    gdw = filtering.backward(ti, w, gw, W, H, f, p0, T(n[None]))
+    gp, _, gs = splatting.backward(W, H, f, gdw, ti, p0, T(n[None]), s0, 0.0)
+    gp, gs = gp.cpu().numpy()[0], gs.cpu().numpy()[0]
+    wr = w.cpu().numpy()
+
+    def fd_points(j, c, eps):
+        a = pts.copy(); a[j, c] += eps
+        b = pts.copy(); b[j, c] -= eps
+        return (loss(T(a[None]), s0) - loss(T(b[None]), s0)) / (2 * eps)
+
+    def fd_sd(j, c, eps):
+        a = sd.copy(); a[0, j, c] += eps
+        b = sd.copy(); b[0, j, c] -= eps
+        return (loss(p0, T(a)) - loss(p0, T(b))) / (2 * eps)
+
+    errs, kinks, checked = [], 0, 0
+    for j in range(N):
+        wj = wr[idx == j]
+        if wj.size == 0 or wj.min() <= 1e-3 or wj.max() >= 1 - 1e-3:
+            continue
+        checked += 1
+        # steps of 0.01 pixel (points) and 0.1 % (std devs)
+        cases = [(fd_points, c, 0.01 * abs(pts[j, 2]) / f, gp[j, c]) for c in range(3)]
+        cases += [(fd_sd, c, 1e-3 * sd[0, j, c], gs[j, c]) for c in range(2)]
+        for fn, c, eps, g in cases:
+            # the depth test of the compositing is piecewise: where a step of
+            # eps moves a splat across another's depth window the loss jumps,
+            # and the two step sizes disagree; such cases are not comparable
+            f1, f2 = fn(j, c, eps), fn(j, c, eps / 2)
+            if abs(f1 - f2) > 0.03 * (abs(f1) + abs(f2)) + 1e-3:
+                kinks += 1
+                continue
+            errs.append((abs(f2 - g) / (abs(f2) + abs(g) + 1e-3), j, c, f1, f2, float(g)))
+        if checked >= 12:
+            break
+    e = np.array([x[0] for x in errs])
+    assert checked >= 8 and len(errs) >= 30 and kinks <= len(errs) // 4, (checked, len(errs), kinks)
+    assert np.median(e) < 1e-2 and e.max() < 0.05, sorted(errs, key=lambda x: -x[0])[:6]
+
+
+def test_sampler_graph_capture(uds):
+    """uds_sample enqueues no host synchronisation and no allocation, so it
+    replays from a CUDA graph (same seed -> same indices)."""
+    from unbiased_differentiable_splatting_gb300.cudaExtensions import sampling
+    sc = _scene(n=2000, W=48)
+    from unbiased_differentiable_splatting_gb300 import scenes
+    P, Nn = scenes.camera_space(sc)
+    P, Nn = P.to(DEV), torch.where(Nn[..., 2:] > 0, -Nn, Nn).contiguous().to(DEV)
+    sd = sc["stddevs"].to(DEV)
+    W = sc["width"]
+    ref = sampling.sample(W, W, sc["focal"], P, Nn, None, sd, 8, 0.0, 0.01, seed=5)
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        sampling.sample(W, W, sc["focal"], P, Nn, None, sd, 8, 0.0, 0.01, seed=5)
+    torch.cuda.current_stream().wait_stream(s)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        out = sampling.sample(W, W, sc["focal"], P, Nn, None, sd, 8, 0.0, 0.01, seed=5)
+    out.fill_(7)
+    g.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(out, ref)

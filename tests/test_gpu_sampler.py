@@ -180,3 +180,27 @@ def test_sample_bad_args(smp):
         smp.sample(8, 8, 8.0, x, x, x, s, 65, 0.0, 0.01)  # K above 64
     with pytest.raises(ValueError):
         smp.sample(8, 8, 8.0, x, x, x, T(np.zeros((2, 4, 2), np.float32)), 4, 0.0, 0.01)
+
+
+@pytest.mark.parametrize("K", [1, 8, 24])
+def test_stochastic_bit_exact(smp, K):
+    """Stochastic mode: indices and path probabilities equal the oracle's."""
+    rng = np.random.default_rng(70 + K)
+    B, W, H, f, N = 2, 40, 36, 36.0, 1500
+    P, Nn = [], []
+    for b in range(B):
+        p, n, s = camera_scene(rng, N, W, H, f)
+        P.append(p)
+        Nn.append(n)
+    sd = rng.uniform(0.005, 0.012, size=(1, N, 2)).astype(np.float32)
+    pts, nrm = np.stack(P), np.stack(Nn)
+    idx, prob, st = smp.sample_stochastic(W, H, f, T(pts), T(nrm), T(sd), K, 0.0, 0.01, seed=99, return_stats=True)
+    idx, prob = idx.cpu().numpy(), prob.cpu().numpy()
+    assert int(st["overflow"].sum()) == 0
+    for b in range(B):
+        ri, rp = oracle.sample_view_stochastic(W, H, f, pts[b], nrm[b], sd[0], K, 0.0, 0.01, h=float(st["h"][b]),
+                                               seed=99, view=b)
+        np.testing.assert_array_equal(idx[b], ri)
+        np.testing.assert_array_equal(prob[b], rp)
+    assert (idx >= 0).mean() > 0.3
+    assert np.all((prob > 0) == (idx >= 0)) and prob.max() <= 1.0

@@ -208,3 +208,48 @@ def test_order_sampling_chi_square():
         pvals.append(chi2.sf(stat, dof))
     # Bonferroni over pixels at alpha = 1e-3
     assert min(pvals) > 1e-3 / len(pvals), pvals
+
+
+def test_stochastic_mode_chi_square():
+    """Stochastic mode: leaf frequencies against the exact FP64 probabilities
+    p_j = G_j(q) / sum_i G_i(q) (direct Gauss sums), and each draw's path
+    probability q against p_j."""
+    from scipy.stats import chi2
+    rng = np.random.default_rng(5)
+    W, H, f, N, K = 20, 20, 18.0, 400, 64
+    pts, nrm, sd = _scene(rng, N, W, H, f, sd=(0.02, 0.05))
+    precision = 1e-6
+    h = oracle.view_bandwidth(W, H, f, pts, nrm, sd, 0.0)
+    t = oracle.Tree(W, H, f, pts, h, oracle.cull_radius(h, precision), precision)
+    e = t.export()
+    n = t.n
+    runs = 80
+    pix = [(i, j) for i in range(3, 18, 5) for j in range(3, 18, 5)]
+    counts = {p: {} for p in pix}
+    qs = {p: {} for p in pix}
+    for s in range(runs):
+        idx, prob = t.sample_stochastic(W, H, K, precision, seed=500 + s)
+        for p in pix:
+            for v, q in zip(idx[p].tolist(), prob[p].tolist()):
+                assert v >= 0 and q > 0
+                counts[p][v] = counts[p].get(v, 0) + 1
+                qs[p][v] = q
+    pvals = []
+    for (i, j) in pix:
+        qq = np.array([i, j], np.float64)
+        total = t.direct_weight(0, qq)
+        exact = {int(e["ids"][L]): t.direct_weight(n - 1 + L, qq) / total for L in range(n)}
+        for v, q in qs[(i, j)].items():
+            if exact[v] > 1e-3:
+                assert abs(q - exact[v]) <= 1e-3 * exact[v] + 1e-6, (v, q, exact[v])
+        ids = sorted(exact, key=lambda v: -exact[v])
+        P = np.array([exact[v] for v in ids])
+        O = np.array([counts[(i, j)].get(v, 0) for v in ids], np.float64)
+        E = runs * K * P
+        big = E >= 5
+        Ob = np.append(O[big], O[~big].sum())
+        Eb = np.append(E[big], E[~big].sum())
+        keep = Eb > 0
+        stat = np.sum((Ob[keep] - Eb[keep]) ** 2 / Eb[keep])
+        pvals.append(chi2.sf(stat, max(int(keep.sum()) - 1, 1)))
+    assert min(pvals) > 1e-3 / len(pvals), pvals

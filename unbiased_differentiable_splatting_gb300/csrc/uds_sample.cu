@@ -941,6 +941,75 @@ __global__ void __launch_bounds__(128) k_sample(Tree T, const ViewState* vs, int
         if (k < K) out[k] = ids[k];
 }
 
+// Stochastic mode (no reference counterpart).  Each of the K draws of a
+// pixel descends from the root into a child with probability
+// m_child / (m_left + m_right), masses by getWeight, and records the product
+// q of the ratios it took: the probability of having drawn that leaf, which
+// importance-weighted estimators divide by.  Draw k at depth d uses Philox
+// counter (pixel, view, 2^31 | k << 8 | d / 4, 0), component d % 4, and steps
+// left iff u <= m_left / (m_left + m_right).  The draws of one pixel share
+// their upper paths, so the child masses of the last path are kept per depth
+// (node ids are unique, so a hit is exact).  A draw that meets two zero
+// masses, or is still above the leaves after kTrace levels, stays -1 / 0.
+__global__ void __launch_bounds__(128) k_stochastic(Tree T, const ViewState* vs, int W, int H, int K,
+                                                    float precision, uint64_t seed, uint32_t view,
+                                                    int* __restrict__ indices, float* __restrict__ probs,
+                                                    uds_view_stats* st) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    int i = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= W || j >= H) return;
+    T.n = vs->n;
+    T.sq = vs->sq;
+    int n = T.n;
+    if (n == 0) return;
+    size_t pixel = (size_t)j + (size_t)H * i;
+    float qx = (float)i, qy = (float)j;
+    if (fmaxf(0.0f, node_weight(T, 0, qx, qy)) < precision) return;
+    int cn[kTrace];
+    float cm0[kTrace], cm1[kTrace];
+    for (int d = 0; d < kTrace; ++d) cn[d] = -1;
+    int* out = indices + (size_t)K * pixel;
+    float* pq = probs + (size_t)K * pixel;
+    bool overflow = false;
+    for (int k = 0; k < K; ++k) {
+        int v = 0, d = 0;
+        float prob = 1.0f;
+        uint32_t c[4];
+        bool ok = true;
+        while (v < n - 1) {
+            if ((d & 3) == 0) {
+                c[0] = (uint32_t)pixel; c[1] = view; c[2] = 0x80000000u | ((uint32_t)k << 8) | (uint32_t)(d >> 2);
+                c[3] = 0;
+                philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+            }
+            float u = bits_to_uniform(c[d & 3]);
+            int4 L = T.lnk[v];
+            float w0, w1;
+            if (cn[d] == v) {
+                w0 = cm0[d];
+                w1 = cm1[d];
+            } else {
+                w0 = fmaxf(0.0f, node_weight(T, L.x, qx, qy));
+                w1 = fmaxf(0.0f, node_weight(T, L.y, qx, qy));
+                cn[d] = v;
+                cm0[d] = w0;
+                cm1[d] = w1;
+            }
+            float sum = fadd(fadd(0.0f, w0), w1);
+            if (!(sum > 0.0f)) { ok = false; break; }
+            float r0 = fdiv(w0, sum);
+            if (u <= r0) { prob = fmul(prob, r0); v = L.x; }
+            else { prob = fmul(prob, fdiv(w1, sum)); v = L.y; }
+            if (++d >= kTrace && v < n - 1) { ok = false; overflow = true; break; }
+        }
+        if (ok) {
+            out[k] = T.leaf_id[v - (n - 1)];
+            pq[k] = prob;
+        }
+    }
+    if (overflow) atomicAdd(&st->overflow, 1);
+}
+
 __global__ void k_finish_view(const ViewState* vs, uds_view_stats* st) {
     st->n_visible = vs->n;
     st->n_coefs = (int)vs->coef_used;
@@ -1077,6 +1146,37 @@ extern "C" int uds_sample(const uds_sample_params* prm, const float* points, con
             case 7: launch_sample<7>(T, w, prm, u, b, idx, s); break;
             default: launch_sample<8>(T, w, prm, u, b, idx, s); break;
         }
+        if ((st = launch_status())) return st;
+    }
+    if (stats) {
+        e = cudaMemcpyAsync(stats, w.stats, sizeof(uds_view_stats) * prm->B, cudaMemcpyDeviceToDevice, s);
+        if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
+    }
+    return UDS_OK;
+}
+
+extern "C" int uds_sample_stochastic(const uds_sample_params* prm, const float* points, const float* normals,
+                                     const float* std_devs, const float* h_override, int32_t* indices,
+                                     float* probs, uds_view_stats* stats, void* workspace, size_t workspace_bytes,
+                                     void* stream) {
+    int st = check_params(prm);
+    if (st) return st;
+    if (!indices || !probs || (prm->N > 0 && (!points || !normals || !std_devs))) return UDS_ERR_ARGUMENT;
+    Ws w = layout(prm, reinterpret_cast<char*>(workspace));
+    if (!workspace || workspace_bytes < w.bytes) return UDS_ERR_WORKSPACE;
+    cudaStream_t s = as_stream(stream);
+    size_t per_view = (size_t)prm->W * prm->H * prm->K;
+    cudaError_t e = cudaMemsetAsync(indices, 0xFF, sizeof(int32_t) * per_view * prm->B, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(probs, 0, sizeof(float) * per_view * prm->B, s);
+    if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
+    Tree T = tree_of(w);
+    dim3 block(16, 8);
+    dim3 grid(cdiv(prm->H, block.x), cdiv(prm->W, block.y));
+    for (int b = 0; b < prm->B; ++b) {
+        if ((st = build_view(prm, w, b, points, normals, std_devs, h_override, s))) return st;
+        if (prm->N == 0) continue;
+        k_stochastic<<<grid, block, 0, s>>>(T, w.vs, prm->W, prm->H, prm->K, prm->precision, prm->seed, (uint32_t)b,
+                                            indices + per_view * b, probs + per_view * b, w.stats + b);
         if ((st = launch_status())) return st;
     }
     if (stats) {

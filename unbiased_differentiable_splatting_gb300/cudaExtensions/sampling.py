@@ -15,6 +15,11 @@ end so existing calls keep working:
 * ``return_stats``: also return the per-view record (h, cull radius, visible
   splats, stored coefficients, demoted nodes, trace overflows) as a (B,8)
   tensor viewed from uds_view_stats.
+
+``sample_stochastic`` is a second sampling mode with no reference
+counterpart: K independent mass-proportional descents per pixel, returning the
+indices and each draw's path probability q (for importance-weighted
+estimators).
 """
 from __future__ import annotations
 
@@ -85,6 +90,35 @@ def sample(width: int, height: int, focallength: float, points, normals, colors,
     if return_stats:
         return indices, view_stats(stats)
     return indices
+
+
+def sample_stochastic(width: int, height: int, focallength: float, points, normals, stdDevs, numSamples: int,
+                      smoothing: float, precision: float, seed=None, h=None, return_stats=False,
+                      max_degree=MAX_DEGREE, coef_pool=0):
+    """K independent draws per pixel, each descending the FGT tree with
+    child-mass-proportional probabilities.  Returns (indices (B,W,H,K) int32,
+    probs (B,W,H,K) float32 path probabilities; -1 / 0 where no draw)."""
+    _check(points, normals, stdDevs)
+    dev = points.device
+    B = points.shape[0]
+    K = int(numSamples)
+    if seed is None:
+        seed = int(torch.randint(0, 2 ** 62, (1,)).item())
+    prm = params(width, height, focallength, points, stdDevs, K, smoothing, precision, seed, max_degree, coef_pool)
+    if h is not None:
+        need(h, "h", device=dev)
+        if h.numel() != B:
+            raise ValueError("h must have B entries")
+    L = load()
+    ws = Workspace.get(dev, workspace_bytes(prm), "sample")
+    indices = torch.empty((B, int(width), int(height), K), dtype=torch.int32, device=dev)
+    probs = torch.empty((B, int(width), int(height), K), dtype=torch.float32, device=dev)
+    stats = torch.empty((B, 8), dtype=torch.float32, device=dev) if return_stats else None
+    check(L.uds_sample_stochastic(prm, ptr(points), ptr(normals), ptr(stdDevs), ptr(h), ptr(indices), ptr(probs),
+                                  ptr(stats), ptr(ws), ws.numel(), stream_ptr(dev)), "sampling sample_stochastic")
+    if return_stats:
+        return indices, probs, view_stats(stats)
+    return indices, probs
 
 
 def view_stats(stats: torch.Tensor) -> dict:
