@@ -60,36 +60,47 @@ def dist_info():
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks / throttle reasons, streamed every 50 ms by one
+    nvidia-smi process (-lms) for the duration of the timed region."""
 
     def __init__(self, index):
         self.index = index
         self.samples = []
-        self._stop = threading.Event()
+        self._proc = None
         self._t = None
 
     def start(self):
+        q = "clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
+            "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
+            "clocks_event_reasons.sw_power_cap"
+        try:
+            self._proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                           "--format=csv,noheader,nounits", "-lms", "50"],
+                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self._proc = None
+            return
+
         def run():
-            q = "clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
-                "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
-                "clocks_event_reasons.sw_power_cap"
-            while not self._stop.is_set():
-                try:
-                    out = subprocess.run(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
-                                          "--format=csv,noheader,nounits"], capture_output=True, text=True,
-                                         timeout=5).stdout.strip()
-                    if out:
-                        self.samples.append([x.strip() for x in out.split(",")])
-                except Exception:
-                    pass
-                self._stop.wait(0.2)
+            for line in self._proc.stdout:
+                line = line.strip()
+                if line:
+                    self.samples.append([x.strip() for x in line.split(",")])
         self._t = threading.Thread(target=run, daemon=True)
         self._t.start()
+        t0 = time.time()
+        while not self.samples and time.time() - t0 < 3.0:  # first sample in before timing starts
+            time.sleep(0.01)
 
     def stop(self):
-        self._stop.set()
+        if self._proc is not None:
+            self._proc.terminate()  # the one process this sampler started
+            try:
+                self._proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self._proc.kill()
         if self._t:
-            self._t.join(timeout=10)
+            self._t.join(timeout=5)
         if not self.samples:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
         sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
@@ -193,6 +204,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="harmonic500k", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--eager", action="store_true", help="time eager steps instead of a CUDA-graph replay")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
@@ -219,7 +231,10 @@ def main():
     S = W * H * K
     opts = RenderOptions(forward="-z", numSamples=K, precision=wl["precision"], shadingMode="forward")
     renderer = Splatting(opts, None, W, H, scene["focal"], 0.1, 100.0, smoothing=0.0).to(dev)
-    renderer.sample_kwargs = {"seed": 1234}
+    # the Philox key lives on the device and advances every step, so each
+    # step (eager or a CUDA-graph replay) draws new uniforms
+    seed_t = torch.tensor([1234], dtype=torch.int64, device=dev)
+    renderer.sample_kwargs = {"seed": seed_t}
     keys = ["cam_positions", "cam_orientations", "points", "normals", "stddevs", "colors", "ambient",
             "lamp_directions", "lamp_intensities"]
     host = {k: scene[k].contiguous().pin_memory() for k in keys}
@@ -238,7 +253,28 @@ def main():
                              inp["lamp_intensities"])
         loss = ((img - target) ** 2).sum()
         loss.backward()
+        seed_t.add_(1)
         return loss
+
+    def capture_graph():
+        """The whole fwd+bwd step as one CUDA graph over static inputs (the
+        recipe of torch.cuda.graph for whole-network capture)."""
+        static = {k: d[k].detach().clone() for k in keys}
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(side):
+            for _ in range(3):
+                for v in static.values():
+                    v.grad = None
+                step(static)
+        torch.cuda.current_stream(dev).wait_stream(side)
+        for v in static.values():
+            v.grad = None
+        graph = torch.cuda.CUDAGraph()
+        n0 = L.uds_launch_count()
+        with torch.cuda.graph(graph):
+            loss = step(static)
+        return graph, static, loss, L.uds_launch_count() - n0
 
     # target image: the scene with positions perturbed by N(0, 0.005)
     with torch.no_grad():
@@ -255,28 +291,51 @@ def main():
         step({k: v.detach().clone() for k, v in d.items()})
     torch.cuda.synchronize(dev)
 
+    graph = None
+    if not args.eager:
+        try:
+            graph, static, static_loss, launches_per_graph = capture_graph()
+            torch.cuda.synchronize(dev)
+        except Exception as e:  # capture is an optimisation; eager stays correct
+            print(f"CUDA graph capture failed, timing eager steps: {e}", file=sys.stderr)
+            graph = None
+            torch.cuda.synchronize(dev)
+
+    def timed_steps(n, use_graph):
+        out = []
+        for _ in range(n):
+            inp = None if use_graph else {k: v.detach().clone() for k, v in d.items()}
+            flush.fill_(1)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            if use_graph:
+                graph.replay()
+            else:
+                step(inp)
+            e1.record(stream)
+            e1.synchronize()
+            out.append(e0.elapsed_time(e1))
+        return out
+
     # ---- value: device-resident inputs
     clocks = ClockSampler(local)
     clocks.start()
-    times = []
     launches0 = L.uds_launch_count()
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize(dev)
-    for _ in range(args.steps):
-        inp = {k: v.detach().clone() for k, v in d.items()}
-        flush.fill_(1)
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        step(inp)
-        e1.record(stream)
-        e1.synchronize()
-        times.append(e0.elapsed_time(e1))
+    times = timed_steps(args.steps, graph is not None)
     torch.cuda.synchronize(dev)
-    launches = (L.uds_launch_count() - launches0) // max(args.steps, 1)
+    if graph is not None:
+        launches = launches_per_graph  # a replay re-runs the captured launches
+    else:
+        launches = (L.uds_launch_count() - launches0) // max(args.steps, 1)
     clk = clocks.stop()
     t_step = float(np.sum(times)) / args.steps  # ms
+    t_eager = t_step
+    if graph is not None:
+        t_eager = float(np.mean(timed_steps(max(3, args.steps // 2), False)))
     if world > 1:
         tt = torch.tensor([t_step], device=dev)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
@@ -285,16 +344,25 @@ def main():
 
     # ---- e2e: host buffers, H2D of every input and D2H of the loss per step
     h2d = sum(v.numel() * v.element_size() for v in host.values())
-    e2e_times = []
-    for _ in range(max(2, args.steps // 2)):
-        flush.fill_(1)
-        torch.cuda.synchronize(dev)
-        t0 = time.perf_counter()
-        inp = {k: v.to(dev, non_blocking=True) for k, v in host.items()}
-        loss = step(inp)
-        float(loss.item())
-        e2e_times.append(time.perf_counter() - t0)
-    t_e2e = float(np.median(e2e_times))
+    def e2e_steps(n, use_graph):
+        out = []
+        for _ in range(n):
+            flush.fill_(1)
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            if use_graph:
+                for k, v in host.items():
+                    static[k].detach().copy_(v, non_blocking=True)
+                graph.replay()
+                float(static_loss.item())
+            else:
+                inp = {k: v.to(dev, non_blocking=True) for k, v in host.items()}
+                float(step(inp).item())
+            out.append(time.perf_counter() - t0)
+        return float(np.median(out))
+
+    t_e2e = e2e_steps(max(2, args.steps // 2), graph is not None)
+    t_e2e_eager = e2e_steps(max(2, args.steps // 2), False) if graph is not None else t_e2e
     if world > 1:
         tt = torch.tensor([t_e2e], device=dev)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
@@ -354,8 +422,12 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": workload_name(args.workload, wl), "l2": "flushed (256 MiB write) before each step",
-                       "parallelism": f"replicas x{world}"},
-            "e2e": {"value": e2e, "unit": "Msamples/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": 4},
+                       "parallelism": f"replicas x{world}", "cuda_graph": graph is not None},
+            "e2e": {"value": e2e, "unit": "Msamples/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": 4,
+                    "path": ("pinned H2D into the captured step's inputs + CUDA-graph replay of Splatting fwd+bwd "
+                             "+ loss D2H" if graph is not None else "pinned H2D + Splatting fwd+bwd + loss D2H"),
+                    "eager_value": world * S / t_e2e_eager / 1e6},
+            "eager_ms_per_step": t_eager,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": profiled_traffic() if args.workload == "harmonic500k" else None,
                          "traffic_source": "ncu capture, profiles/k_sample_k_p2m_harmonic500k_1024.md",

@@ -64,6 +64,10 @@ typedef struct {
     int32_t std_batch;       /* leading dim of stdDevs: 1 or B */
     int64_t coef_pool;       /* coefficient pool size in floats (<=0: default) */
     uint64_t seed;           /* Philox key when `uniforms` is NULL */
+    const uint64_t* seed_dev;/* optional device pointer: when set, the key is
+                                read from it at kernel run time instead of
+                                `seed`, so a captured CUDA graph draws new
+                                numbers after the caller updates it */
 } uds_sample_params;
 
 /* ---- transform (transform.cpp:33-86: affineForward/Backward,

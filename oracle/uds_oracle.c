@@ -1056,7 +1056,10 @@ orc_tree* orc_tree_build(int W, int H, float f, int N, const float* pts, float h
     t->coef = (float*)calloc((size_t)(total > 0 ? total : 1), sizeof(float));
     /* P2M (HermiteCoefficientFunctor + shiftLeafHermiteExpansion,
      * buildDynamicRadixTree.cuh:280-313, hermitefmm.cuh:119-138): each node
-     * sums its leaves' terms in leaf order */
+     * sums its leaves' terms in leaf order.  The libm flavour evaluates each
+     * term as the reference does, (1 * s0^a * s1^b) / (a! b!); the
+     * deterministic flavour (the GPU's arithmetic) builds t_a = s^a / a! by
+     * the recurrence t_a = (t_{a-1} * s) / a and adds fma(tx_a, ty_b, C_ab). */
     float sq = sqrtf(2.0f * h * h);
     for (int v = 0; v < L0; ++v) {
         int p = t->degree[v];
@@ -1065,11 +1068,23 @@ orc_tree* orc_tree_build(int W, int H, float f, int N, const float* pts, float h
         for (int i = t->first[v]; i <= t->last[v]; ++i) {
             float s0 = (t->leafxy[2 * i] - t->centre[2 * v]) / sq;
             float s1 = (t->leafxy[2 * i + 1] - t->centre[2 * v + 1]) / sq;
-            for (int x = 0; x <= p; ++x)
-                for (int y = 0; y <= p; ++y) {
-                    float term = (1.0f * (xpowi(s0, (unsigned)x, fl) * xpowi(s1, (unsigned)y, fl))) / (facf((unsigned)x) * facf((unsigned)y));
-                    C[x * (p + 1) + y] += term;
+            if (fl == ORC_LIBM) {
+                for (int x = 0; x <= p; ++x)
+                    for (int y = 0; y <= p; ++y) {
+                        float term = (1.0f * (xpowi(s0, (unsigned)x, fl) * xpowi(s1, (unsigned)y, fl))) / (facf((unsigned)x) * facf((unsigned)y));
+                        C[x * (p + 1) + y] += term;
+                    }
+            } else {
+                float tx[ORC_MAXDEGREE + 1], ty[ORC_MAXDEGREE + 1];
+                tx[0] = 1.0f;
+                ty[0] = 1.0f;
+                for (int a = 1; a <= p; ++a) {
+                    tx[a] = (tx[a - 1] * s0) / (float)a;
+                    ty[a] = (ty[a - 1] * s1) / (float)a;
                 }
+                for (int x = 0; x <= p; ++x)
+                    for (int y = 0; y <= p; ++y) C[x * (p + 1) + y] = fmaf(tx[x], ty[y], C[x * (p + 1) + y]);
+            }
         }
     }
     /* truncation radius per node (truncate, evaluateDynamicRadixTree.cuh:118-126) */

@@ -186,3 +186,30 @@ def test_sampler_graph_capture(uds):
     g.replay()
     torch.cuda.synchronize()
     assert torch.equal(out, ref)
+
+
+def test_sampler_graph_device_seed(uds):
+    """With the Philox key in a device tensor, one captured graph draws the
+    samples of whatever key the tensor holds at replay time."""
+    from unbiased_differentiable_splatting_gb300.cudaExtensions import sampling
+    from unbiased_differentiable_splatting_gb300 import scenes
+    sc = _scene(n=2000, W=48)
+    P, Nn = scenes.camera_space(sc)
+    P, Nn = P.to(DEV), torch.where(Nn[..., 2:] > 0, -Nn, Nn).contiguous().to(DEV)
+    sd = sc["stddevs"].to(DEV)
+    W = sc["width"]
+    seed = torch.tensor([41], dtype=torch.int64, device=DEV)
+    ref41 = sampling.sample(W, W, sc["focal"], P, Nn, None, sd, 8, 0.0, 0.01, seed=41)
+    ref42 = sampling.sample(W, W, sc["focal"], P, Nn, None, sd, 8, 0.0, 0.01, seed=42)
+    assert not torch.equal(ref41, ref42)
+    assert torch.equal(sampling.sample(W, W, sc["focal"], P, Nn, None, sd, 8, 0.0, 0.01, seed=seed), ref41)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        out = sampling.sample(W, W, sc["focal"], P, Nn, None, sd, 8, 0.0, 0.01, seed=seed)
+        seed.add_(1)
+    g.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(out, ref41) and int(seed.item()) == 42
+    g.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(out, ref42)

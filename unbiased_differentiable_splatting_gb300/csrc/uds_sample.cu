@@ -527,12 +527,25 @@ __global__ void k_assign(ViewState* vs, float4* cen, const uint32_t* __restrict_
 
 // ----------------------------------------------------------------- 7 P2M
 // shiftLeafHermiteExpansion (hermitefmm.cuh:119-138) summed per node over
-// its leaves in Morton order.  One warp per internal node.
-__global__ void k_p2m(const ViewState* vs, const int4* __restrict__ lnk, const float4* __restrict__ cen,
-                      const float2* __restrict__ leaf_xy, float* __restrict__ coef) {
+// its leaves in Morton order: C_ab = sum_i t_a(s0_i) t_b(s1_i) with
+// t_a(s) = s^a / a!, s = (leaf - centre) / sqrt(2 h^2).  One warp per
+// internal node.  For a chunk of 32 leaves each lane builds one leaf's
+// t-tables in shared memory (t_a = (t_{a-1} s) / a); lane (g, b) then owns
+// column b and rows a = g, g + G, ... (G = 32 / (p+1) row groups) and adds
+// fma(t_a(s0), t_b(s1), C_ab) leaf by leaf, so every coefficient is summed in
+// leaf order exactly as the oracle's deterministic flavour does.
+constexpr int kP2MWarps = 4;
+constexpr int kTStride = kMaxDegree + 1;  // odd: conflict-free row writes
+
+__global__ void __launch_bounds__(32 * kP2MWarps) k_p2m(const ViewState* vs, const int4* __restrict__ lnk,
+                                                        const float4* __restrict__ cen,
+                                                        const float2* __restrict__ leaf_xy,
+                                                        float* __restrict__ coef) {
+    __shared__ float s_tx[kP2MWarps][32 * kTStride];
+    __shared__ float s_ty[kP2MWarps][32 * kTStride];
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int v = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    int lane = threadIdx.x & 31;
-    if (v >= vs->n - 1) return;
+    if (v >= vs->n - 1) return;  // uniform over the warp
     float4 c = cen[v];
     int p = meta_degree(c.w);
     if (p < 0) return;
@@ -540,19 +553,47 @@ __global__ void k_p2m(const ViewState* vs, const int4* __restrict__ lnk, const f
     int4 L = lnk[v];
     float sq = vs->sq;
     int P1 = p + 1;
-    for (int k = lane; k < P1 * P1; k += 32) {
-        unsigned a = (unsigned)(k / P1), b = (unsigned)(k % P1);
-        float fab = fmul(facf(a), facf(b));
-        float sum = 0.0f;
-        for (int i = L.z; i < L.z + L.w; ++i) {
-            float2 q = leaf_xy[i];
+    int G = 32 / P1;
+    int b = lane % P1, g = lane / P1;
+    bool owner = g < G;
+    int nrows = owner ? (P1 - g + G - 1) / G : 0;
+    float acc[kMaxDegree + 1];
+#pragma unroll
+    for (int r = 0; r <= kMaxDegree; ++r) acc[r] = 0.0f;
+    float* tx = s_tx[warp];
+    float* ty = s_ty[warp];
+    int end = L.z + L.w;
+    for (int i0 = L.z; i0 < end; i0 += 32) {
+        int cnt = min(32, end - i0);
+        if (lane < cnt) {
+            float2 q = leaf_xy[i0 + lane];
             float s0 = fdiv(fsub(q.x, c.x), sq);
             float s1 = fdiv(fsub(q.y, c.y), sq);
-            float term = fdiv(fmul(1.0f, fmul(ipowf(s0, a), ipowf(s1, b))), fab);
-            sum = fadd(sum, term);
+            float ax = 1.0f, ay = 1.0f;
+            tx[lane * kTStride] = 1.0f;
+            ty[lane * kTStride] = 1.0f;
+            for (int a = 1; a <= p; ++a) {
+                ax = fdiv(fmul(ax, s0), (float)a);
+                ay = fdiv(fmul(ay, s1), (float)a);
+                tx[lane * kTStride + a] = ax;
+                ty[lane * kTStride + a] = ay;
+            }
         }
-        coef[off + k] = sum;
+        __syncwarp();
+        if (owner) {
+            for (int j = 0; j < cnt; ++j) {
+                float yb = ty[j * kTStride + b];
+                const float* row = tx + j * kTStride + g;
+#pragma unroll
+                for (int r = 0; r <= kMaxDegree; ++r)
+                    if (r < nrows) acc[r] = __fmaf_rn(row[r * G], yb, acc[r]);
+            }
+        }
+        __syncwarp();
     }
+#pragma unroll
+    for (int r = 0; r <= kMaxDegree; ++r)
+        if (r < nrows) coef[off + (g + r * G) * P1 + b] = acc[r];
 }
 
 // -------------------------------------------------------- FGT evaluation
@@ -770,9 +811,10 @@ __device__ void warp_root_walk(const Tree& T, float qx, float qy, bool live, Mas
 template <int R, int KM>
 __global__ void __launch_bounds__(128) k_sample(Tree T, const ViewState* vs, int W, int H, int K,
                                                 float precision, const float* __restrict__ uniforms,
-                                                uint64_t seed, uint32_t view, int* __restrict__ indices,
-                                                uds_view_stats* st) {
+                                                uint64_t seed, const uint64_t* __restrict__ seed_ptr,
+                                                uint32_t view, int* __restrict__ indices, uds_view_stats* st) {
     // block 8 (y) x 16 (x); warp = 8 x 4 pixel tile
+    if (seed_ptr) seed = *seed_ptr;
     __shared__ WalkStack s_walk[4];
     const unsigned full = 0xffffffffu;
     int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -952,12 +994,14 @@ __global__ void __launch_bounds__(128) k_sample(Tree T, const ViewState* vs, int
 // (node ids are unique, so a hit is exact).  A draw that meets two zero
 // masses, or is still above the leaves after kTrace levels, stays -1 / 0.
 __global__ void __launch_bounds__(128) k_stochastic(Tree T, const ViewState* vs, int W, int H, int K,
-                                                    float precision, uint64_t seed, uint32_t view,
+                                                    float precision, uint64_t seed,
+                                                    const uint64_t* __restrict__ seed_ptr, uint32_t view,
                                                     int* __restrict__ indices, float* __restrict__ probs,
                                                     uds_view_stats* st) {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     int i = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= W || j >= H) return;
+    if (seed_ptr) seed = *seed_ptr;
     T.n = vs->n;
     T.sq = vs->sq;
     int n = T.n;
@@ -1089,10 +1133,12 @@ static void launch_sample(const Tree& T, const Ws& w, const uds_sample_params* p
     dim3 grid(cdiv(p->H, block.x), cdiv(p->W, block.y));
     if (R <= 3 && p->K <= 8)
         k_sample<(R <= 3 ? R : 3), 8><<<grid, block, 0, s>>>(T, w.vs, p->W, p->H, p->K, p->precision, u, p->seed,
+                                                             p->seed_dev,
                                                              (uint32_t)view, idx, w.stats + view);
     else
         k_sample<(R >= 3 ? R : 3), kMaxK><<<grid, block, 0, s>>>(T, w.vs, p->W, p->H, p->K, p->precision, u,
-                                                                 p->seed, (uint32_t)view, idx, w.stats + view);
+                                                                 p->seed, p->seed_dev, (uint32_t)view, idx,
+                                                                 w.stats + view);
 }
 
 static int check_params(const uds_sample_params* p) {
@@ -1175,7 +1221,7 @@ extern "C" int uds_sample_stochastic(const uds_sample_params* prm, const float* 
     for (int b = 0; b < prm->B; ++b) {
         if ((st = build_view(prm, w, b, points, normals, std_devs, h_override, s))) return st;
         if (prm->N == 0) continue;
-        k_stochastic<<<grid, block, 0, s>>>(T, w.vs, prm->W, prm->H, prm->K, prm->precision, prm->seed, (uint32_t)b,
+        k_stochastic<<<grid, block, 0, s>>>(T, w.vs, prm->W, prm->H, prm->K, prm->precision, prm->seed, prm->seed_dev, (uint32_t)b,
                                             indices + per_view * b, probs + per_view * b, w.stats + b);
         if ((st = launch_status())) return st;
     }

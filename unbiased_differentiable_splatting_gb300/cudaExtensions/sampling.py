@@ -9,7 +9,9 @@ end so existing calls keep working:
   numbers consumed by the order sampling (round-major per pixel, candidates in
   Morton order).  Without it Philox4x32-10 uniforms are drawn from ``seed``
   (the reference seeds curand with time(NULL)).
-* ``seed``: 64-bit Philox key; default draws one from torch's CPU generator.
+* ``seed``: 64-bit Philox key, or a one-element int64 CUDA tensor holding it
+  (read on the device, for CUDA-graph replay); default draws one from
+  torch's CPU generator.
 * ``h``: (B,) float32 CUDA tensor of bandwidths that replace the computed ones
   (entries <= 0 keep the computed value).
 * ``return_stats``: also return the per-view record (h, cull radius, visible
@@ -38,10 +40,20 @@ def num_rounds(K: int) -> int:
 
 def params(width, height, focallength, points, stdDevs, numSamples, smoothing, precision, seed=0,
            max_degree=MAX_DEGREE, coef_pool=0) -> SampleParams:
-    return SampleParams(B=points.shape[0], N=points.shape[1], W=int(width), H=int(height), K=int(numSamples),
-                        focal=float(focallength), smoothing=float(smoothing), precision=float(precision),
-                        max_degree=int(max_degree), std_batch=stdDevs.shape[0], coef_pool=int(coef_pool or 0),
-                        seed=int(seed) & 0xFFFFFFFFFFFFFFFF)
+    """``seed``: an int, or a one-element int64 CUDA tensor whose value the
+    kernels read when they run (a captured CUDA graph then draws new numbers
+    after the tensor is updated)."""
+    prm = SampleParams(B=points.shape[0], N=points.shape[1], W=int(width), H=int(height), K=int(numSamples),
+                       focal=float(focallength), smoothing=float(smoothing), precision=float(precision),
+                       max_degree=int(max_degree), std_batch=stdDevs.shape[0], coef_pool=int(coef_pool or 0),
+                       seed=0, seed_dev=None)
+    if isinstance(seed, torch.Tensor):
+        if seed.dtype != torch.int64 or seed.numel() != 1 or seed.device != points.device:
+            raise ValueError("a seed tensor must be one int64 element on the points' device")
+        prm.seed_dev = seed.data_ptr()
+    else:
+        prm.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
+    return prm
 
 
 def workspace_bytes(prm: SampleParams) -> int:

@@ -47,7 +47,9 @@ def world2Camera(camPositions: th.Tensor, camQuaternion: th.Tensor) -> th.Tensor
 def transformForward(viewMatrix: th.Tensor, forward: str) -> th.Tensor:
     """utils.py:51-60: for forward == 'z' flip y and mirror z."""
     if forward == "z":
-        flip = th.diag(th.tensor([1.0, -1.0, -1.0, 1.0], dtype=viewMatrix.dtype, device=viewMatrix.device))
+        d = th.ones(4, dtype=viewMatrix.dtype, device=viewMatrix.device)
+        d[1:3] = -1.0  # built on the device: no host copy, so CUDA-graph capture works
+        flip = th.diag(d)
         viewMatrix = flip.view(1, 1, 4, 4) @ viewMatrix
     return viewMatrix
 
