@@ -629,12 +629,44 @@ __device__ __forceinline__ float hermite_eval(const Tree& T, int v, float4 c, fl
     for (int k = 2; k <= kMaxDegree; ++k)
         if (k <= p) hy[k] = fsub(fmul(ty2, hy[k - 1]), fmul(fmul(2.0f, (float)(k - 1)), hy[k - 2]));
     float tx2 = fmul(2.0f, tx);
-    float hxm2 = 0.0f, hxm1 = 0.0f, hx = ex;
+    float hxm2 = 0.0f, hxm1 = 0.0f;
     float w = 0.0f;
-    for (int a = 0; a <= p; ++a) {
-        if (a == 1) hx = fmul(tx2, ex);
-        else if (a >= 2) hx = fsub(fmul(tx2, hxm1), fmul(fmul(2.0f, (float)(a - 1)), hxm2));
-        const float* Ca = C + a * (p + 1);
+    const int P1 = p + 1;
+    int a = 0;
+    // Rows four at a time: the four row sums are independent chains, so they
+    // are interleaved; each chain and the outer sum keep their order.
+    for (; a + 4 <= P1; a += 4) {
+        float h[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            int aa = a + q;
+            float hx = aa == 0 ? ex
+                               : (aa == 1 ? fmul(tx2, ex)
+                                          : fsub(fmul(tx2, hxm1), fmul(fmul(2.0f, (float)(aa - 1)), hxm2)));
+            h[q] = hx;
+            hxm2 = hxm1;
+            hxm1 = hx;
+        }
+        const float* C0 = C + a * P1;
+        float r0 = 0.0f, r1 = 0.0f, r2 = 0.0f, r3 = 0.0f;
+#pragma unroll
+        for (int b = 0; b <= kMaxDegree; ++b) {
+            if (b <= p) {
+                r0 = __fmaf_rn(C0[b], hy[b], r0);
+                r1 = __fmaf_rn(C0[P1 + b], hy[b], r1);
+                r2 = __fmaf_rn(C0[2 * P1 + b], hy[b], r2);
+                r3 = __fmaf_rn(C0[3 * P1 + b], hy[b], r3);
+            }
+        }
+        w = __fmaf_rn(h[0], r0, w);
+        w = __fmaf_rn(h[1], r1, w);
+        w = __fmaf_rn(h[2], r2, w);
+        w = __fmaf_rn(h[3], r3, w);
+    }
+    for (; a <= p; ++a) {
+        float hx = a == 0 ? ex
+                          : (a == 1 ? fmul(tx2, ex) : fsub(fmul(tx2, hxm1), fmul(fmul(2.0f, (float)(a - 1)), hxm2)));
+        const float* Ca = C + a * P1;
         float r = 0.0f;
 #pragma unroll
         for (int b = 0; b <= kMaxDegree; ++b)
