@@ -42,6 +42,19 @@ WORKLOADS = {
     "sphere4k": dict(scene="sphere", n=4096, width=128, K=8, precision=0.01),
 }
 
+# Multi-view workloads (timed by multiview_main; not the default bench line):
+# groups of views sharing one resolution, rendered into one loss per step.
+MULTIVIEW = {
+    # 2M surfels on the walls of a 5 x 5 x 3 m room + 40 boxes, 16 interior
+    # views 640x480 (f = 525 px), poses perturbed by N(0, 0.01 rad / 0.02 m);
+    # gradients for the splats and the 6-DoF poses
+    "room16": dict(n=2_000_000, K=8, precision=0.01, shading="forward", groups=[(640, 480, 525.0, 16)]),
+    # 300k surfels with 8 N(0,1) feature channels (no shading), views of four
+    # resolutions: 8 x 256^2, 4 x 128^2, 4 x 512^2, 4 x 1024x768 (60 deg fov)
+    "features20": dict(n=300_000, K=8, precision=0.01, shading="None",
+                       groups=[(256, 256, None, 8), (128, 128, None, 4), (512, 512, None, 4), (1024, 768, None, 4)]),
+}
+
 
 def make_scene(wl):
     from unbiased_differentiable_splatting_gb300 import scenes
@@ -196,16 +209,133 @@ def reference_arm(args, wl, name):
     }), flush=True)
 
 
+def multiview_main(args, name, wl):
+    """Several views (possibly of different resolutions) per step: one
+    Splatting module per resolution group, one summed L2 loss, backward to the
+    splats and the camera poses; the whole step captured as one CUDA graph."""
+    import torch
+    from unbiased_differentiable_splatting_gb300 import load, scenes
+    from unbiased_differentiable_splatting_gb300.render import RenderOptions, Splatting
+    if args.impl == "reference":
+        print(json.dumps({"impl": "reference", "unavailable": "multi-view workloads are timed for this build only; "
+                          "the reference arm times the default workload"}))
+        return
+    L = load()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    K = wl["K"]
+    nviews = sum(g[3] for g in wl["groups"])
+    if name == "room16":
+        sc = scenes.room_scene(n=wl["n"], views=nviews, seed=0)
+        rng = np.random.default_rng(1)
+        # perturbed poses: 0.01 rad about a random axis, 0.02 m
+        q = sc["cam_orientations"].numpy().astype(np.float64)
+        ax = rng.normal(size=(nviews, 3))
+        ax /= np.linalg.norm(ax, axis=1, keepdims=True)
+        dq = np.concatenate([ax * math.sin(0.005), np.full((nviews, 1), math.cos(0.005))], 1)
+        x1, y1, z1, w1 = dq.T
+        x2, y2, z2, w2 = q.T
+        qp = np.stack([w1 * x2 + x1 * w2 + y1 * z2 - z1 * y2, w1 * y2 - x1 * z2 + y1 * w2 + z1 * x2,
+                       w1 * z2 + x1 * y2 - y1 * x2 + z1 * w2, w1 * w2 - x1 * x2 - y1 * y2 - z1 * z2], 1)
+        pert_q = torch.from_numpy(qp.astype(np.float32))
+        pert_t = sc["cam_positions"] + torch.from_numpy(rng.normal(0, 0.02, size=(nviews, 3)).astype(np.float32))
+    else:
+        sc = scenes.feature_scene(n=wl["n"], channels=8, seed=0)
+        cp, co = scenes.orbit_cameras(nviews, distance=2.0, seed=0)
+        sc.update(cam_positions=cp, cam_orientations=co)
+        ld, li, amb = scenes._lights(nviews)
+        sc.update(lamp_directions=ld, lamp_intensities=li, ambient=amb)
+        pert_q, pert_t = co.clone(), cp.clone()
+    d = {k: v.to(dev) for k, v in sc.items() if isinstance(v, torch.Tensor)}
+    seed_t = torch.tensor([99], dtype=torch.int64, device=dev)
+    groups, v0 = [], 0
+    for (W, H, f, nv) in wl["groups"]:
+        f = f if f is not None else scenes.focal_from_fov(W)
+        opts = RenderOptions(forward="-z", numSamples=K, precision=wl["precision"], shadingMode=wl["shading"])
+        r = Splatting(opts, None, W, H, f, 0.1, 100.0, smoothing=0.0).to(dev)
+        r.sample_kwargs = {"seed": seed_t}
+        groups.append((r, slice(v0, v0 + nv), W, H))
+        v0 += nv
+    S = sum(W * H * (sl.stop - sl.start) * K for _, sl, W, H in groups)
+
+    def render(pos, quat, pts, nrm, sd, col):
+        out = []
+        for r, sl, W, H in groups:
+            img, _, _ = r(pos[sl], quat[sl], pts, nrm, sd, col, d["ambient"], d["lamp_directions"][sl],
+                          d["lamp_intensities"])
+            out.append(img)
+        return out
+
+    with torch.no_grad():
+        targets = [t.detach() for t in render(d["cam_positions"], d["cam_orientations"], d["points"], d["normals"],
+                                              d["stddevs"], d["colors"])]
+    static = dict(pos=pert_t.to(dev), quat=pert_q.to(dev), pts=d["points"].clone(), nrm=d["normals"].clone(),
+                  sd=d["stddevs"].clone(), col=d["colors"].clone())
+
+    def step():
+        for k in ("pos", "quat", "pts", "sd", "col"):
+            static[k].requires_grad_(True)
+        imgs = render(static["pos"], static["quat"], static["pts"], static["nrm"], static["sd"], static["col"])
+        loss = sum(((a - b) ** 2).sum() for a, b in zip(imgs, targets))
+        loss.backward()
+        seed_t.add_(1)
+        return loss
+
+    side = torch.cuda.Stream(dev)
+    side.wait_stream(torch.cuda.current_stream(dev))
+    with torch.cuda.stream(side):
+        for _ in range(max(args.warmup, 3)):
+            for v in static.values():
+                v.grad = None
+            step()
+    torch.cuda.current_stream(dev).wait_stream(side)
+    for v in static.values():
+        v.grad = None
+    graph = torch.cuda.CUDAGraph()
+    n0 = L.uds_launch_count()
+    with torch.cuda.graph(graph):
+        static_loss = step()
+    launches = L.uds_launch_count() - n0
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    clocks = ClockSampler(0)
+    clocks.start()
+    times = []
+    for _ in range(args.steps):
+        flush.fill_(1)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        graph.replay()
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    clk = clocks.stop()
+    t = float(np.mean(times))
+    g = static["quat"].grad
+    print(json.dumps({
+        "metric": "fwd+bwd Msamples/s", "value": S / (t * 1e-3) / 1e6, "unit": "Msamples/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": name, "views": [f"{sl.stop - sl.start}x{W}x{H}" for _, sl, W, H in groups],
+                   "samples_per_step": S, "surfels": wl["n"], "K": K, "shading": wl["shading"],
+                   "l2": "flushed (256 MiB write) before each step", "cuda_graph": True},
+        "loss": float(static_loss.item()), "pose_grad_finite": bool(torch.isfinite(g).all().item()) if g is not None
+        else None, "clocks": clk, "gpu_launches": int(launches)}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="harmonic500k", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="harmonic500k", choices=sorted(WORKLOADS) + sorted(MULTIVIEW))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--eager", action="store_true", help="time eager steps instead of a CUDA-graph replay")
     args = ap.parse_args()
+    if args.workload in MULTIVIEW:
+        return multiview_main(args, args.workload, MULTIVIEW[args.workload])
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
         return reference_arm(args, wl, args.workload)

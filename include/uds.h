@@ -62,7 +62,8 @@ typedef struct {
     float precision;         /* FGT truncation precision */
     int32_t max_degree;      /* cap of the adaptive Hermite degree (<= 16) */
     int32_t std_batch;       /* leading dim of stdDevs: 1 or B */
-    int64_t coef_pool;       /* coefficient pool size in floats (<=0: default) */
+    int64_t coef_pool;       /* coefficient pool size in floats, < 2^26 (<=0: default
+                                64 per splat, at least 2^20, at most 2^26 - 1) */
     uint64_t seed;           /* Philox key when `uniforms` is NULL */
     const uint64_t* seed_dev;/* optional device pointer: when set, the key is
                                 read from it at kernel run time instead of

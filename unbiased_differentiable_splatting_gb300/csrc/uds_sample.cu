@@ -66,7 +66,13 @@ struct Ws {
 
 static size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-static int64_t default_pool(int64_t N) { return N * 64 > (1 << 20) ? N * 64 : (1 << 20); }
+// Default coefficient pool: 64 floats per splat, at least 2^20, at most the
+// 2^26 - 1 that the 26-bit offsets of the node metadata can address (nodes
+// past the pool are demoted to subtree walks, as the oracle does).
+static int64_t default_pool(int64_t N) {
+    int64_t p = N * 64 > (1 << 20) ? N * 64 : (1 << 20);
+    return p < (1ll << 26) ? p : (1ll << 26) - 1;
+}
 
 static Ws layout(const uds_sample_params* p, char* base) {
     Ws w{};

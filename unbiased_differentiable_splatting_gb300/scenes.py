@@ -198,6 +198,24 @@ def room_scene(n=2_000_000, views=16, width=640, height=480, focal=525.0, n_boxe
                 lamp_intensities=li, ambient=amb, width=width, height=height, focal=focal)
 
 
+def orbit_cameras(views: int, distance: float = 2.0, seed: int = 0):
+    """`views` cameras at `distance` from the origin in random directions of
+    the upper hemisphere (z > 0.2 of the unit direction), each looking at the
+    origin: (cam_positions (views,3) world->camera translations,
+    cam_orientations (views,4) quaternions)."""
+    rng = np.random.default_rng(seed)
+    cams, quats = [], []
+    while len(cams) < views:
+        d = _unit_directions(rng, 1)[0]
+        if d[2] < 0.2:
+            continue
+        c = distance * d
+        q, Rw = _quat_look(-c)
+        cams.append(-Rw @ c)
+        quats.append(q)
+    return _t(np.array(cams)), _t(np.array(quats))
+
+
 def camera_space(scene, device="cpu"):
     """Camera-space points / normals (B,N,3) of a scene (same transform as
     ``Splatting.forward`` for forward '-z'), for calling the ops directly."""
