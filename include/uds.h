@@ -126,8 +126,10 @@ int uds_fgt_eval(const uds_sample_params* prm, int m, const int32_t* nodes, cons
 
 /* ---- splatting.forward / backward (splatting.cpp:43-129).  points,
  *      normals (B,N,3) camera space; std_devs (std_batch,N,2); weights and
- *      grad (B,W,H,K).  Workspace: per-splat Gaussian constants and gradient
- *      statistics, uds_splat_workspace_size(B, N) bytes. ---- */
+ *      grad (B,W,H,K).  Workspace: per-splat Gaussian constants, gradient
+ *      statistics and a flag per (view, splat) pair, uds_splat_workspace_size(B, N)
+ *      bytes.  Only pairs that some pixel samples are evaluated; the others
+ *      get zero gradients, as in the reference. ---- */
 size_t uds_splat_workspace_size(int B, int N);
 int uds_splat_forward(int B, int W, int H, int K, float focal, const int32_t* indices,
                       const float* points, const float* normals, int std_batch, int N,

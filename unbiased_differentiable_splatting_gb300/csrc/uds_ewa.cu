@@ -16,11 +16,12 @@ namespace uds {
 __global__ void k_ewa_consts(int B, int N, float W, float H, float f,
                              const float* __restrict__ pts, const float* __restrict__ nrm,
                              const float* __restrict__ sd, int sdB, float sm,
-                             float4* __restrict__ consts) {
+                             const unsigned char* __restrict__ used, float4* __restrict__ consts) {
     int x = blockIdx.x * blockDim.x + threadIdx.x;
     int b = blockIdx.y;
     if (x >= N) return;
     size_t o = (size_t)x + (size_t)N * b;
+    if (!used[o]) return;  // no pixel of view b samples splat x
     float p[3] = {pts[3 * o], pts[3 * o + 1], pts[3 * o + 2]};
     float n[3] = {nrm[3 * o], nrm[3 * o + 1], nrm[3 * o + 2]};
     size_t so = sdB > 1 ? o : (size_t)x;
@@ -31,6 +32,23 @@ __global__ void k_ewa_consts(int B, int N, float W, float H, float f,
     ewa_gauss_consts(F, a, c);
     consts[2 * o] = a;
     consts[2 * o + 1] = c;
+}
+
+// Flag the (view, splat) pairs that some pixel samples: only those need the
+// Gaussian constants (their frame takes double-precision divisions, which
+// are slow on this GPU), and only those receive gradient, as in the
+// reference, whose kernels visit sampled pairs only.
+__global__ void k_ewa_mark(int B, int W, int H, int K, const int* __restrict__ idx, int N,
+                           unsigned char* __restrict__ used) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    int i = blockIdx.y;
+    int b = blockIdx.z;
+    if (j >= H) return;
+    size_t pix = (size_t)j + (size_t)H * ((size_t)i + (size_t)W * b);
+    for (int s = 0; s < K; ++s) {
+        int id = idx[(size_t)s + (size_t)K * pix];
+        if (id >= 0 && id < N) used[(size_t)id + (size_t)N * b] = 1;
+    }
 }
 
 // One thread per pixel (x = i, y = j), K samples.
@@ -196,8 +214,10 @@ using namespace uds;
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// Workspace: Gaussian constants (2 float4 per pair), gradient statistics (2
+// float4 per pair), one flag byte per pair.
 extern "C" size_t uds_splat_workspace_size(int B, int N) {
-    return align256(sizeof(float4) * 2 * (size_t)B * N) * 2;
+    return align256(sizeof(float4) * 2 * (size_t)B * N) * 2 + align256((size_t)B * N);
 }
 
 static int check_splat_args(int B, int W, int H, int K, int std_batch, int N) {
@@ -217,9 +237,14 @@ extern "C" int uds_splat_forward(int B, int W, int H, int K, float focal, const 
     cudaStream_t s = as_stream(stream);
     float4* consts = reinterpret_cast<float4*>(workspace);
     if (N > 0) {
+        unsigned char* used = reinterpret_cast<unsigned char*>(workspace) +
+                              2 * align256(sizeof(float4) * 2 * (size_t)B * N);
+        cudaError_t e = cudaMemsetAsync(used, 0, (size_t)B * N, s);
+        if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
+        k_ewa_mark<<<dim3(cdiv(H, 64), W, B), 64, 0, s>>>(B, W, H, K, indices, N, used);
         k_ewa_consts<<<dim3(cdiv(N, 128), B), 128, 0, s>>>(B, N, (float)W, (float)H, focal, points, normals,
-                                                          std_devs, std_batch, smoothing, consts);
-        if ((st = launch_status())) return st;
+                                                          std_devs, std_batch, smoothing, used, consts);
+        if ((st = launch_status(2))) return st;
     }
     k_ewa_forward<<<dim3(cdiv(H, 64), W, B), 64, 0, s>>>(B, W, H, K, indices, consts, N, weights);
     return launch_status();
@@ -242,10 +267,14 @@ extern "C" int uds_splat_backward(int B, int W, int H, int K, float focal, const
     cudaError_t e = cudaMemsetAsync(stats, 0, sizeof(float4) * 2 * (size_t)B * N, s);
     if (e == cudaSuccess && std_batch == 1)
         e = cudaMemsetAsync(grad_std_devs, 0, sizeof(float) * 2 * (size_t)N, s);
+    unsigned char* used = reinterpret_cast<unsigned char*>(workspace) +
+                          2 * align256(sizeof(float4) * 2 * (size_t)B * N);
+    if (e == cudaSuccess) e = cudaMemsetAsync(used, 0, (size_t)B * N, s);
     if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
+    k_ewa_mark<<<dim3(cdiv(H, 64), W, B), 64, 0, s>>>(B, W, H, K, indices, N, used);
     k_ewa_consts<<<dim3(cdiv(N, 128), B), 128, 0, s>>>(B, N, (float)W, (float)H, focal, points, normals,
-                                                      std_devs, std_batch, smoothing, consts);
-    if ((st = launch_status())) return st;
+                                                      std_devs, std_batch, smoothing, used, consts);
+    if ((st = launch_status(2))) return st;
     k_ewa_stats<<<dim3(cdiv(H, 64), W, B), 64, 0, s>>>(B, W, H, K, grad, indices, consts, N, stats);
     if ((st = launch_status())) return st;
     k_ewa_chain<<<dim3(cdiv(N, 128), B), 128, 0, s>>>(B, N, (float)W, (float)H, focal, points, normals,

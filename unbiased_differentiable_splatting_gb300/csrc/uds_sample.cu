@@ -306,10 +306,11 @@ __global__ void k_radix_scatter(int N, const uint32_t* __restrict__ kin, const u
 }
 
 // ------------------------------------------------ generic exclusive scan
-__global__ void k_scan_reduce(const uint32_t* __restrict__ in, const ViewState* vs, int minus,
+// Length: vs->n - minus when vs is given, else M0.
+__global__ void k_scan_reduce(const uint32_t* __restrict__ in, const ViewState* vs, int minus, int M0,
                               uint32_t* __restrict__ part) {
     __shared__ uint32_t red[kScanThreads / 32];
-    int M = vs->n - minus;
+    int M = vs ? vs->n - minus : M0;
     size_t base = (size_t)blockIdx.x * kScanTile;
     uint32_t s = 0;
     for (int r = 0; r < kScanItems; ++r) {
@@ -350,10 +351,11 @@ __global__ void k_scan_top(uint32_t* part, int nb) {
     if (t == blockDim.x - 1) part[nb] = buf[t];  // total
 }
 
-__global__ void k_scan_down(const uint32_t* __restrict__ in, const ViewState* vs, int minus,
-                            const uint32_t* __restrict__ part, uint32_t* __restrict__ out) {
+// in and out may be the same array (each thread reads its items first).
+__global__ void k_scan_down(const uint32_t* in, const ViewState* vs, int minus, int M0, const uint32_t* part,
+                            uint32_t* out) {
     __shared__ uint32_t wsum[kScanThreads / 32];
-    int M = vs->n - minus;
+    int M = vs ? vs->n - minus : M0;
     size_t base = (size_t)blockIdx.x * kScanTile + (size_t)threadIdx.x * kScanItems;
     uint32_t v[kScanItems], local = 0;
 #pragma unroll
@@ -1134,9 +1136,19 @@ static int build_view(const uds_sample_params* p, const Ws& w, int view, const f
     for (int pass = 0; pass < 4; ++pass) {
         int shift = 8 * pass;
         k_radix_hist<<<nb, kSortThreads, 0, s>>>(N, ki, shift, w.hist);
-        k_radix_scan<<<1, 1024, 0, s>>>(w.hist, (int)(256 * nb));
+        int nh = (int)(256 * nb);
+        int launched = 3;
+        if (nh <= 16 * 1024) {
+            k_radix_scan<<<1, 1024, 0, s>>>(w.hist, nh);
+        } else {  // many tiles: the three-phase multi-block scan
+            unsigned hb = cdiv(nh, kScanTile);
+            k_scan_reduce<<<hb, kScanThreads, 0, s>>>(w.hist, nullptr, 0, nh, w.scanTmp);
+            k_scan_top<<<1, 1024, 0, s>>>(w.scanTmp, (int)hb);
+            k_scan_down<<<hb, kScanThreads, 0, s>>>(w.hist, nullptr, 0, nh, w.scanTmp, w.hist);
+            launched = 5;
+        }
         k_radix_scatter<<<nb, kSortThreads, 0, s>>>(N, ki, vi, ko, vo, shift, w.hist);
-        if ((st = launch_status(3))) return st;
+        if ((st = launch_status(launched))) return st;
         uint32_t* t = ki; ki = ko; ko = t;
         t = vi; vi = vo; vo = t;
     }
@@ -1148,9 +1160,9 @@ static int build_view(const uds_sample_params* p, const Ws& w, int view, const f
     k_node_sizes<<<nbN, 128, 0, s>>>(w.vs, w.cen, w.sizes);
     if ((st = launch_status(4))) return st;
     unsigned sb = cdiv(N, kScanTile);
-    k_scan_reduce<<<sb, kScanThreads, 0, s>>>(w.sizes, w.vs, 1, w.scanTmp);
+    k_scan_reduce<<<sb, kScanThreads, 0, s>>>(w.sizes, w.vs, 1, 0, w.scanTmp);
     k_scan_top<<<1, 1024, 0, s>>>(w.scanTmp, (int)sb);
-    k_scan_down<<<sb, kScanThreads, 0, s>>>(w.sizes, w.vs, 1, w.scanTmp, w.offsets);
+    k_scan_down<<<sb, kScanThreads, 0, s>>>(w.sizes, w.vs, 1, 0, w.scanTmp, w.offsets);
     k_assign<<<nbN, 128, 0, s>>>(w.vs, w.cen, w.sizes, w.offsets, w.coef_cap, w.stats + view);
     k_p2m<<<cdiv((size_t)N * 32, 128), 128, 0, s>>>(w.vs, w.lnk, w.cen, w.leaf_xy, w.coef);
     k_finish_view<<<1, 1, 0, s>>>(w.vs, w.stats + view);
