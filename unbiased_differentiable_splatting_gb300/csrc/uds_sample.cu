@@ -605,6 +605,11 @@ __global__ void __launch_bounds__(32 * kP2MWarps) k_p2m(const ViewState* vs, con
 }
 
 // -------------------------------------------------------- FGT evaluation
+template <typename P>
+__device__ __forceinline__ const P* shifted(const P* p, size_t bytes) {
+    return reinterpret_cast<const P*>(reinterpret_cast<const char*>(p) + bytes);
+}
+
 struct Tree {
     const int4* lnk;
     const int* par;
@@ -849,12 +854,30 @@ __device__ void warp_root_walk(const Tree& T, float qx, float qy, bool live, Mas
 }
 
 template <int R, int KM>
-__global__ void __launch_bounds__(128) k_sample(Tree T, const ViewState* vs, int W, int H, int K,
+__global__ void __launch_bounds__(128, 3) k_sample(Tree T, const ViewState* vs, int W, int H, int K,
                                                 float precision, const float* __restrict__ uniforms,
                                                 uint64_t seed, const uint64_t* __restrict__ seed_ptr,
-                                                uint32_t view, int* __restrict__ indices, uds_view_stats* st) {
-    // block 8 (y) x 16 (x); warp = 8 x 4 pixel tile
+                                                uint32_t view, int* __restrict__ indices, uds_view_stats* st,
+                                                size_t vstride, size_t ustride, size_t istride) {
+    // block 8 (y) x 16 (x); warp = 8 x 4 pixel tile.  blockIdx.z selects the
+    // view: its tree lives vstride bytes after the previous view's, its
+    // uniforms ustride floats and its indices istride entries further on.
     if (seed_ptr) seed = *seed_ptr;
+    if (blockIdx.z) {
+        size_t off = (size_t)blockIdx.z * vstride;
+        T.lnk = shifted(T.lnk, off);
+        T.par = shifted(T.par, off);
+        T.box = shifted(T.box, off);
+        T.cen = shifted(T.cen, off);
+        T.coef = shifted(T.coef, off);
+        T.leaf_xy = shifted(T.leaf_xy, off);
+        T.leaf_id = shifted(T.leaf_id, off);
+        vs = shifted(vs, off);
+        view += blockIdx.z;
+        indices += (size_t)blockIdx.z * istride;
+        if (uniforms) uniforms += (size_t)blockIdx.z * ustride;
+        st += blockIdx.z;
+    }
     __shared__ WalkStack s_walk[4];
     const unsigned full = 0xffffffffu;
     int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1177,18 +1200,22 @@ static Tree tree_of(const Ws& w) {
 }
 
 template <int R>
+// Descent for views view .. view + nviews - 1 in one launch (grid.z = view),
+// their trees vstride bytes apart in the workspace.
 static void launch_sample(const Tree& T, const Ws& w, const uds_sample_params* p, const float* u, int view,
-                          int* idx, cudaStream_t s) {
+                          int* idx, cudaStream_t s, int nviews = 1, size_t vstride = 0) {
     dim3 block(8, 16);
-    dim3 grid(cdiv(p->H, block.x), cdiv(p->W, block.y));
+    dim3 grid(cdiv(p->H, block.x), cdiv(p->W, block.y), nviews);
+    size_t istride = (size_t)p->W * p->H * p->K;
+    size_t ustride = (size_t)p->W * p->H * R * p->K;
     if (R <= 3 && p->K <= 8)
         k_sample<(R <= 3 ? R : 3), 8><<<grid, block, 0, s>>>(T, w.vs, p->W, p->H, p->K, p->precision, u, p->seed,
-                                                             p->seed_dev,
-                                                             (uint32_t)view, idx, w.stats + view);
+                                                             p->seed_dev, (uint32_t)view, idx, w.stats + view,
+                                                             vstride, ustride, istride);
     else
         k_sample<(R >= 3 ? R : 3), kMaxK><<<grid, block, 0, s>>>(T, w.vs, p->W, p->H, p->K, p->precision, u,
                                                                  p->seed, p->seed_dev, (uint32_t)view, idx,
-                                                                 w.stats + view);
+                                                                 w.stats + view, vstride, ustride, istride);
 }
 
 static int check_params(const uds_sample_params* p) {
@@ -1207,9 +1234,11 @@ static int check_params(const uds_sample_params* p) {
 
 using namespace uds;
 
+// uds_sample keeps every view's tree resident (one slot per view) so that one
+// descent launch covers all views; the other entry points use slot 0.
 extern "C" size_t uds_sample_workspace_size(const uds_sample_params* prm) {
     if (check_params(prm)) return 0;
-    return layout(prm, nullptr).bytes;
+    return layout(prm, nullptr).bytes * (size_t)prm->B;
 }
 
 extern "C" int uds_sample(const uds_sample_params* prm, const float* points, const float* normals,
@@ -1219,28 +1248,33 @@ extern "C" int uds_sample(const uds_sample_params* prm, const float* points, con
     int st = check_params(prm);
     if (st) return st;
     if (!indices || (prm->N > 0 && (!points || !normals || !std_devs))) return UDS_ERR_ARGUMENT;
-    Ws w = layout(prm, reinterpret_cast<char*>(workspace));
-    if (!workspace || workspace_bytes < w.bytes) return UDS_ERR_WORKSPACE;
+    char* base = reinterpret_cast<char*>(workspace);
+    Ws w = layout(prm, base);
+    size_t slot = w.bytes;
+    if (!workspace || workspace_bytes < slot * (size_t)prm->B) return UDS_ERR_WORKSPACE;
     cudaStream_t s = as_stream(stream);
     size_t per_view = (size_t)prm->W * prm->H * prm->K;
     cudaError_t e = cudaMemsetAsync(indices, 0xFF, sizeof(int32_t) * per_view * prm->B, s);
     if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
-    int R = num_rounds(prm->K);
-    Tree T = tree_of(w);
+    // every view's tree in its own slot (the per-view record stays in slot 0)
     for (int b = 0; b < prm->B; ++b) {
-        if ((st = build_view(prm, w, b, points, normals, std_devs, h_override, s))) return st;
-        if (prm->N == 0) continue;
-        const float* u = uniforms ? uniforms + per_view / prm->K * R * prm->K * b : nullptr;
-        int* idx = indices + per_view * b;
-        switch (R) {
-            case 1: launch_sample<1>(T, w, prm, u, b, idx, s); break;
-            case 2: launch_sample<2>(T, w, prm, u, b, idx, s); break;
-            case 3: launch_sample<3>(T, w, prm, u, b, idx, s); break;
-            case 4: launch_sample<4>(T, w, prm, u, b, idx, s); break;
-            case 5: launch_sample<5>(T, w, prm, u, b, idx, s); break;
-            case 6: launch_sample<6>(T, w, prm, u, b, idx, s); break;
-            case 7: launch_sample<7>(T, w, prm, u, b, idx, s); break;
-            default: launch_sample<8>(T, w, prm, u, b, idx, s); break;
+        Ws wb = layout(prm, base + slot * (size_t)b);
+        wb.stats = w.stats;
+        if ((st = build_view(prm, wb, b, points, normals, std_devs, h_override, s))) return st;
+    }
+    if (prm->N > 0) {
+        // one descent launch over all views
+        Tree T = tree_of(w);
+        int B = prm->B;
+        switch (num_rounds(prm->K)) {
+            case 1: launch_sample<1>(T, w, prm, uniforms, 0, indices, s, B, slot); break;
+            case 2: launch_sample<2>(T, w, prm, uniforms, 0, indices, s, B, slot); break;
+            case 3: launch_sample<3>(T, w, prm, uniforms, 0, indices, s, B, slot); break;
+            case 4: launch_sample<4>(T, w, prm, uniforms, 0, indices, s, B, slot); break;
+            case 5: launch_sample<5>(T, w, prm, uniforms, 0, indices, s, B, slot); break;
+            case 6: launch_sample<6>(T, w, prm, uniforms, 0, indices, s, B, slot); break;
+            case 7: launch_sample<7>(T, w, prm, uniforms, 0, indices, s, B, slot); break;
+            default: launch_sample<8>(T, w, prm, uniforms, 0, indices, s, B, slot); break;
         }
         if ((st = launch_status())) return st;
     }
