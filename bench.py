@@ -257,6 +257,21 @@ def multiview_main(args, name, wl):
         groups.append((r, slice(v0, v0 + nv), W, H))
         v0 += nv
     S = sum(W * H * (sl.stop - sl.start) * K for _, sl, W, H in groups)
+    # autotune the descent's warp tile per resolution group (on its first view)
+    from unbiased_differentiable_splatting_gb300 import autotune
+    from unbiased_differentiable_splatting_gb300.extensions import transformForward, world2Camera
+    from unbiased_differentiable_splatting_gb300.cudaExtensions import transform
+    tiles = []
+    with torch.no_grad():
+        for r, sl, W, H in groups:
+            v = slice(sl.start, sl.start + 1)
+            M = transformForward(world2Camera(d["cam_positions"][v], d["cam_orientations"][v]), "-z").squeeze(1)
+            cp = transform.affineForward(M.contiguous(), d["points"])
+            cn = transform.linearForward(M.contiguous(), d["normals"])
+            cnb = torch.where(cn[..., 2:] > 0, -cn, cn).contiguous()
+            best, _ = autotune.tune_descent(W, H, r.focallength, cp, cnb, d["stddevs"], K, 0.0, wl["precision"])
+            # the cache is keyed by the view's splat count, which is N for every view
+            tiles.append(best)
 
     def render(pos, quat, pts, nrm, sd, col):
         out = []
@@ -318,6 +333,7 @@ def multiview_main(args, name, wl):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": name, "views": [f"{sl.stop - sl.start}x{W}x{H}" for _, sl, W, H in groups],
+                   "descent_tiles": tiles,
                    "samples_per_step": S, "surfels": wl["n"], "K": K, "shading": wl["shading"],
                    "l2": "flushed (256 MiB write) before each step", "cuda_graph": True},
         "loss": float(static_loss.item()), "pose_grad_finite": bool(torch.isfinite(g).all().item()) if g is not None
@@ -416,6 +432,18 @@ def main():
                                 pert["lamp_intensities"])
         target = target.detach()
 
+    # autotune the descent's warp tile on this view (cached per GPU and shape;
+    # the sampler picks it up from the cache)
+    from unbiased_differentiable_splatting_gb300 import autotune
+    from unbiased_differentiable_splatting_gb300.extensions import transformForward, world2Camera
+    from unbiased_differentiable_splatting_gb300.cudaExtensions import transform
+    with torch.no_grad():
+        M = transformForward(world2Camera(d["cam_positions"], d["cam_orientations"]), "-z").squeeze(1).contiguous()
+        cp = transform.affineForward(M, d["points"])
+        cn = transform.linearForward(M, d["normals"])
+        cnb = torch.where(cn[..., 2:] > 0, -cn, cn).contiguous()
+        tile, tile_ms = autotune.tune_descent(W, H, scene["focal"], cp, cnb, d["stddevs"], K, 0.0, wl["precision"])
+
     stream = torch.cuda.current_stream(dev)
     for _ in range(args.warmup):
         step({k: v.detach().clone() for k, v in d.items()})
@@ -501,15 +529,10 @@ def main():
 
     # ---- roofline of the dominant kernel: the per-pixel descent alone
     with torch.no_grad():
-        from unbiased_differentiable_splatting_gb300.extensions import transformForward, world2Camera
-        M = transformForward(world2Camera(d["cam_positions"], d["cam_orientations"]), "-z").squeeze(1).contiguous()
-        from unbiased_differentiable_splatting_gb300.cudaExtensions import transform
-        cp = transform.affineForward(M, d["points"])
-        cn = transform.linearForward(M, d["normals"])
-        cnb = torch.where(cn[..., 2:] > 0, -cn, cn).contiguous()
         tree = sampling.build_tree(W, H, scene["focal"], cp, cnb, d["stddevs"], K, 0.0, wl["precision"])
         prm = tree["_prm"]
         prm.seed = 1234
+        prm.tile_x = tile
         ws = tree["_ws"]
         idx = torch.full((W, H, K), -1, dtype=torch.int32, device=dev)
         for _ in range(2):
@@ -552,7 +575,9 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": workload_name(args.workload, wl), "l2": "flushed (256 MiB write) before each step",
-                       "parallelism": f"replicas x{world}", "cuda_graph": graph is not None},
+                       "parallelism": f"replicas x{world}", "cuda_graph": graph is not None,
+                       "descent_tile": f"{tile}x{32 // tile} pixels per warp (autotuned: "
+                                       + ", ".join(f"{k}: {v:.3f} ms" for k, v in sorted(tile_ms.items())) + ")"},
             "e2e": {"value": e2e, "unit": "Msamples/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": 4,
                     "path": ("pinned H2D into the captured step's inputs + CUDA-graph replay of Splatting fwd+bwd "
                              "+ loss D2H" if graph is not None else "pinned H2D + Splatting fwd+bwd + loss D2H"),

@@ -69,6 +69,10 @@ typedef struct {
                                 read from it at kernel run time instead of
                                 `seed`, so a captured CUDA graph draws new
                                 numbers after the caller updates it */
+    int32_t tile_x;          /* descent warp tile width in pixels along y:
+                                4, 8, 16 or 32 (0 = 8); results do not depend
+                                on it, only speed (see the autotuner) */
+    int32_t reserved0;
 } uds_sample_params;
 
 /* ---- transform (transform.cpp:33-86: affineForward/Backward,

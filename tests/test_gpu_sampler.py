@@ -204,3 +204,23 @@ def test_stochastic_bit_exact(smp, K):
         np.testing.assert_array_equal(prob[b], rp)
     assert (idx >= 0).mean() > 0.3
     assert np.all((prob > 0) == (idx >= 0)) and prob.max() <= 1.0
+
+
+def test_descent_tile_shapes_agree_and_autotune(smp, tmp_path, monkeypatch):
+    """Every warp-tile shape of the descent gives the same indices; the
+    autotuner times them and caches one."""
+    from unbiased_differentiable_splatting_gb300 import autotune
+    monkeypatch.setenv("UDS_AUTOTUNE_CACHE", str(tmp_path / "cache.json"))
+    autotune.reset()
+    rng = np.random.default_rng(80)
+    W, H, f, N, K = 72, 56, 60.0, 3000, 8
+    pts, nrm, sd = camera_scene(rng, N, W, H, f)
+    args = (W, H, f, T(pts[None]), T(nrm[None]), T(np.zeros((1, N, 3))), T(sd[None]), K, 0.0, 0.01)
+    ref = smp.sample(*args, seed=3, tile_x=8)
+    for tx in (4, 16, 32):
+        assert torch.equal(smp.sample(*args, seed=3, tile_x=tx), ref), tx
+    best, times = autotune.tune_descent(W, H, f, T(pts[None]), T(nrm[None]), T(sd[None]), K, 0.0, 0.01)
+    assert best in autotune.CANDIDATES and set(times) == set(autotune.CANDIDATES)
+    assert autotune.lookup(torch.cuda.get_device_name(0), W, H, N, K) == best
+    assert torch.equal(smp.sample(*args, seed=3), ref)  # now with the tuned tile
+    autotune.reset()

@@ -859,7 +859,7 @@ __global__ void __launch_bounds__(128, 3) k_sample(Tree T, const ViewState* vs, 
                                                 uint64_t seed, const uint64_t* __restrict__ seed_ptr,
                                                 uint32_t view, int* __restrict__ indices, uds_view_stats* st,
                                                 size_t vstride, size_t ustride, size_t istride) {
-    // block 8 (y) x 16 (x); warp = 8 x 4 pixel tile.  blockIdx.z selects the
+    // block tile_x (y) x 128 / tile_x (x).  blockIdx.z selects the
     // view: its tree lives vstride bytes after the previous view's, its
     // uniforms ustride floats and its indices istride entries further on.
     if (seed_ptr) seed = *seed_ptr;
@@ -1202,9 +1202,13 @@ static Tree tree_of(const Ws& w) {
 template <int R>
 // Descent for views view .. view + nviews - 1 in one launch (grid.z = view),
 // their trees vstride bytes apart in the workspace.
+// Block: 128 threads, tile_x (y) by 128 / tile_x (x) pixels; each warp is a
+// tile_x by 32 / tile_x pixel tile.  Every lane's walk is its own, so the
+// indices do not depend on the tile shape, only the speed does.
 static void launch_sample(const Tree& T, const Ws& w, const uds_sample_params* p, const float* u, int view,
                           int* idx, cudaStream_t s, int nviews = 1, size_t vstride = 0) {
-    dim3 block(8, 16);
+    int tx = p->tile_x > 0 ? p->tile_x : 8;
+    dim3 block(tx, 128 / tx);
     dim3 grid(cdiv(p->H, block.x), cdiv(p->W, block.y), nviews);
     size_t istride = (size_t)p->W * p->H * p->K;
     size_t ustride = (size_t)p->W * p->H * R * p->K;
@@ -1225,6 +1229,8 @@ static int check_params(const uds_sample_params* p) {
     if (p->std_batch != 1 && p->std_batch != p->B) return UDS_ERR_ARGUMENT;
     if (!(p->precision > 0.0f) || !(p->focal > 0.0f)) return UDS_ERR_ARGUMENT;
     if ((size_t)p->N * 2 >= (1u << 31)) return UDS_ERR_ARGUMENT;
+    if (p->tile_x != 0 && p->tile_x != 4 && p->tile_x != 8 && p->tile_x != 16 && p->tile_x != 32)
+        return UDS_ERR_ARGUMENT;
     int64_t pool = p->coef_pool > 0 ? p->coef_pool : default_pool(p->N);
     if (pool >= (1ll << 26)) return UDS_ERR_ARGUMENT;  // offsets are packed in 26 bits
     return UDS_OK;

@@ -14,6 +14,9 @@ end so existing calls keep working:
   torch's CPU generator.
 * ``h``: (B,) float32 CUDA tensor of bandwidths that replace the computed ones
   (entries <= 0 keep the computed value).
+* ``tile_x``: width of the descent's 32-pixel warp tiles (4, 8, 16, 32);
+  default: the autotuner's cached choice for this shape (see ``autotune``),
+  else 8.  The indices do not depend on it.
 * ``return_stats``: also return the per-view record (h, cull radius, visible
   splats, stored coefficients, demoted nodes, trace overflows) as a (B,8)
   tensor viewed from uds_view_stats.
@@ -39,14 +42,14 @@ def num_rounds(K: int) -> int:
 
 
 def params(width, height, focallength, points, stdDevs, numSamples, smoothing, precision, seed=0,
-           max_degree=MAX_DEGREE, coef_pool=0) -> SampleParams:
+           max_degree=MAX_DEGREE, coef_pool=0, tile_x=0) -> SampleParams:
     """``seed``: an int, or a one-element int64 CUDA tensor whose value the
     kernels read when they run (a captured CUDA graph then draws new numbers
     after the tensor is updated)."""
     prm = SampleParams(B=points.shape[0], N=points.shape[1], W=int(width), H=int(height), K=int(numSamples),
                        focal=float(focallength), smoothing=float(smoothing), precision=float(precision),
                        max_degree=int(max_degree), std_batch=stdDevs.shape[0], coef_pool=int(coef_pool or 0),
-                       seed=0, seed_dev=None)
+                       seed=0, seed_dev=None, tile_x=int(tile_x or 0), reserved0=0)
     if isinstance(seed, torch.Tensor):
         if seed.dtype != torch.int64 or seed.numel() != 1 or seed.device != points.device:
             raise ValueError("a seed tensor must be one int64 element on the points' device")
@@ -74,16 +77,34 @@ def _check(points, normals, stdDevs):
         raise ValueError("stdDevs must be (1|B,N,2)")
 
 
+def _tile(points, width, height, numSamples, tile_x):
+    """Descent tile width: the given one, else the autotuner's cached choice
+    for this shape, else the default."""
+    if tile_x:
+        return int(tile_x)
+    from .. import autotune
+    dev = points.device
+    name = _device_names.get(dev.index)
+    if name is None:
+        name = _device_names[dev.index] = torch.cuda.get_device_name(dev)
+    t = autotune.lookup(name, width, height, points.shape[1], numSamples)
+    return t or autotune.DEFAULT_TILE
+
+
+_device_names = {}
+
+
 def sample(width: int, height: int, focallength: float, points, normals, colors, stdDevs, numSamples: int,
            smoothing: float, precision: float, uniforms=None, seed=None, h=None, return_stats=False,
-           max_degree=MAX_DEGREE, coef_pool=0):
+           max_degree=MAX_DEGREE, coef_pool=0, tile_x=None):
     _check(points, normals, stdDevs)
     dev = points.device
     B = points.shape[0]
     K = int(numSamples)
     if seed is None:
         seed = int(torch.randint(0, 2 ** 62, (1,)).item())
-    prm = params(width, height, focallength, points, stdDevs, K, smoothing, precision, seed, max_degree, coef_pool)
+    prm = params(width, height, focallength, points, stdDevs, K, smoothing, precision, seed, max_degree, coef_pool,
+                 _tile(points, width, height, K, tile_x))
     if uniforms is not None:
         need(uniforms, "uniforms", device=dev)
         R = num_rounds(K)
