@@ -128,6 +128,22 @@ int uds_sample_descent(const uds_sample_params* prm, int view, const float* unif
 int uds_fgt_eval(const uds_sample_params* prm, int m, const int32_t* nodes, const float* query_xy,
                  float* out, const void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---- proposal network (no counterpart in the reference).  Tensor-core
+ *      kernels (tcgen05, accumulators in tensor memory). ---- */
+/* Layout check of the tensor-core path (debug): C (128 x N, fp32) =
+ * A (128 x K, bf16) * B (N x K, bf16)^T, 16 <= N <= 64, 16 <= K <= 128, both
+ * multiples of 16; swap selects the reading of the two descriptor distances;
+ * *err (device int, preset to 0) becomes 1 if the product did not complete. */
+int uds_mma_probe(int N, int K, const uint16_t* A, const uint16_t* B, float* C, int swap, int* err,
+                  void* stream);
+
+/* Proposal network 16 -> 64 -> 64 -> 64 -> 2 (ReLU), parameters fp32 in one
+ * array of uds_mlp_param_count() floats: W1 (64x16), b1, W2 (64x64), b2,
+ * W3 (64x64), b3, W4 (16x64, rows 2..15 zero), b4 (16).  Computed in bf16
+ * with fp32 accumulation.  uds_mlp_forward: X (R x 16) -> logits (R x 2). */
+int uds_mlp_param_count(void);
+int uds_mlp_forward(int R, const float* X, const float* params, float* logits, int* err, void* stream);
+
 /* ---- splatting.forward / backward (splatting.cpp:43-129).  points,
  *      normals (B,N,3) camera space; std_devs (std_batch,N,2); weights and
  *      grad (B,W,H,K).  Workspace: per-splat Gaussian constants, gradient
