@@ -143,6 +143,15 @@ int uds_mma_probe(int N, int K, const uint16_t* A, const uint16_t* B, float* C, 
  * with fp32 accumulation.  uds_mlp_forward: X (R x 16) -> logits (R x 2). */
 int uds_mlp_param_count(void);
 int uds_mlp_forward(int R, const float* X, const float* params, float* logits, int* err, void* stream);
+/* Training: adds the gradient of the mean cross-entropy between
+ * softmax(logits) and (target, 1 - target) over the R rows to grad (fp32,
+ * uds_mlp_param_count() entries, zeroed by the caller) and the mean loss to
+ * *loss (device float).  uds_mlp_adam: one Adam step (bias-corrected, step
+ * >= 1) on params with moments m1, m2; consumes (zeroes) grad. */
+int uds_mlp_grad(int R, const float* X, const float* target, const float* params, float* grad, float* loss,
+                 int* err, void* stream);
+int uds_mlp_adam(float* params, float* grad, float* m1, float* m2, int step, float lr, float beta1, float beta2,
+                 float eps, void* stream);
 
 /* ---- splatting.forward / backward (splatting.cpp:43-129).  points,
  *      normals (B,N,3) camera space; std_devs (std_batch,N,2); weights and

@@ -83,3 +83,67 @@ def test_mlp_forward(L, R):
     assert int(err.item()) == 0
     d = (out.cpu() - ref).abs().max() / ref.abs().max()
     assert d < 1e-2, float(d)  # bf16 activations: rounding may differ in the last bit
+
+
+def torch_loss(P, X, target):
+    """Mean cross-entropy of the torch reference (bf16-rounded operands)."""
+    logits = torch_forward(P, X)
+    logq = torch.log_softmax(logits, -1)
+    return -(target * logq[:, 0] + (1 - target) * logq[:, 1]).mean()
+
+
+@pytest.mark.parametrize("R", [128, 5000])
+def test_mlp_grad(L, R):
+    n = L.uds_mlp_param_count()
+    P = init_params(n, seed=7)
+    g = torch.Generator().manual_seed(R)
+    X = torch.randn(R, 16, generator=g)
+    target = torch.rand(R, generator=g)
+    Pr = P.clone().requires_grad_(True)
+    loss = torch_loss(Pr, X, target)
+    loss.backward()
+    ref = Pr.grad
+    G = torch.zeros(n, device=DEV)
+    lo = torch.zeros(1, device=DEV)
+    err = torch.zeros(1, dtype=torch.int32, device=DEV)
+    Pd, Xd, td = P.to(DEV), X.to(DEV), target.to(DEV)
+    assert L.uds_mlp_grad(R, Xd.data_ptr(), td.data_ptr(), Pd.data_ptr(), G.data_ptr(), lo.data_ptr(),
+                          err.data_ptr(), torch.cuda.current_stream().cuda_stream) == 0
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    assert abs(float(lo.item()) - float(loss)) < 1e-3 * abs(float(loss)) + 1e-4
+    Gc = G.cpu()
+    o = 0
+    for (r, c) in ((64, 16), (64, 64), (64, 64), (16, 64)):
+        for size in (r * c, r):
+            a, b = Gc[o:o + size], ref[o:o + size]
+            rel = float((a - b).norm() / (b.norm() + 1e-12))
+            assert rel < 0.03, (o, size, rel)  # bf16 rounding of the backward operands
+            o += size
+
+
+def test_mlp_training_reduces_loss(L):
+    """A few hundred Adam steps on a smooth target drive the loss down."""
+    n = L.uds_mlp_param_count()
+    P = init_params(n, seed=3).to(DEV)
+    m1 = torch.zeros(n, device=DEV)
+    m2 = torch.zeros(n, device=DEV)
+    G = torch.zeros(n, device=DEV)
+    g = torch.Generator(device=DEV).manual_seed(0)
+    X = torch.randn(20000, 16, device=DEV, generator=g)
+    target = torch.sigmoid(2.0 * X[:, 0] - X[:, 1] + 0.5 * X[:, 2] * X[:, 3])
+    err = torch.zeros(1, dtype=torch.int32, device=DEV)
+    s = torch.cuda.current_stream().cuda_stream
+    losses = []
+    for step in range(1, 301):
+        lo = torch.zeros(1, device=DEV)
+        assert L.uds_mlp_grad(X.shape[0], X.data_ptr(), target.data_ptr(), P.data_ptr(), G.data_ptr(), lo.data_ptr(),
+                              err.data_ptr(), s) == 0
+        assert L.uds_mlp_adam(P.data_ptr(), G.data_ptr(), m1.data_ptr(), m2.data_ptr(), step, 3e-3, 0.9, 0.999,
+                              1e-8, s) == 0
+        if step in (1, 300):
+            losses.append(float(lo.item()))
+    assert int(err.item()) == 0
+    # entropy floor of the soft targets
+    floor = float(-(target * target.log() + (1 - target) * (1 - target).log()).mean())
+    assert losses[1] - floor < 0.25 * (losses[0] - floor), (losses, floor)

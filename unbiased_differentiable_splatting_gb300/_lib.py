@@ -56,6 +56,9 @@ _SIGS = {
     "uds_mma_probe": (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_void_p]),
     "uds_mlp_param_count": (c_int, []),
     "uds_mlp_forward": (c_int, [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "uds_mlp_grad": (c_int, [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "uds_mlp_adam": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_float, c_float, c_float, c_float,
+                             c_void_p]),
     "uds_splat_workspace_size": (c_size_t, [c_int, c_int]),
     "uds_splat_forward": (c_int, [c_int, c_int, c_int, c_int, c_float, c_void_p, c_void_p, c_void_p, c_int,
                                   c_int, c_void_p, c_float, c_void_p, c_void_p, c_size_t, c_void_p]),

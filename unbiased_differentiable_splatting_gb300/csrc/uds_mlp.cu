@@ -228,6 +228,299 @@ __global__ void __launch_bounds__(128) k_mlp_forward(int R, const float* __restr
     if (warp == 0) tc::tmem_dealloc(taddr, 64);
 }
 
+// ------------------------------------------------------------ training
+// Gradient of the mean cross-entropy between the branch distribution
+// softmax(logits) and the target (p, 1 - p) over R rows, added to G (fp32,
+// kParams entries; the caller zeroes it) and the loss added to loss[0].
+// Per 128-row tile: the forward pass keeps the three hidden activations in
+// shared memory; the backward pass runs dH = dZ * W on the tensor cores
+// (B operand: W transposed, staged once) and the weight and bias gradients
+// (reductions over the batch rows) on the CUDA cores, accumulated in
+// registers across the CTA's tiles and added to G once at the end.
+struct MlpGradSmem {
+    __align__(1024) unsigned char w1[mlp::kHid * mlp::kIn * 2];
+    __align__(1024) unsigned char w2[mlp::kHid * mlp::kHid * 2];
+    __align__(1024) unsigned char w3[mlp::kHid * mlp::kHid * 2];
+    __align__(1024) unsigned char w4[mlp::kOut * mlp::kHid * 2];
+    __align__(1024) unsigned char w2t[mlp::kHid * mlp::kHid * 2];
+    __align__(1024) unsigned char w3t[mlp::kHid * mlp::kHid * 2];
+    __align__(1024) unsigned char w4t[mlp::kHid * mlp::kOut * 2];
+    __align__(1024) unsigned char x[mlp::kTile * mlp::kIn * 2];
+    __align__(1024) unsigned char h[3][mlp::kTile * mlp::kHid * 2];
+    __align__(1024) unsigned char dz[2][mlp::kTile * mlp::kHid * 2];
+    __align__(1024) unsigned char dz4[mlp::kTile * mlp::kOut * 2];
+    float dz4f[mlp::kTile][2];
+    float bias[3 * mlp::kHid + mlp::kOut];
+    float dbias[3 * mlp::kHid + mlp::kOut];
+    float loss;
+    uint64_t mbar;
+    uint32_t taddr;
+};
+
+__device__ __forceinline__ float get_bf16(const unsigned char* base, uint32_t off) {
+    return __bfloat162float(*reinterpret_cast<const __nv_bfloat16*>(base + off));
+}
+
+// 8 consecutive K elements (k0 multiple of 8) of row r of a K-major operand.
+__device__ __forceinline__ void get8(const unsigned char* base, int r, int k0, int K, float (&v)[8]) {
+    uint4 q = *reinterpret_cast<const uint4*>(base + tc::kmajor_offset(r, k0, K));
+    const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&q);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        float2 f = __bfloat1622float2(h[i]);
+        v[2 * i] = f.x;
+        v[2 * i + 1] = f.y;
+    }
+}
+
+// Stage W (R x K, fp32 row-major) transposed: operand of K rows x R columns.
+__device__ __forceinline__ void stage_transposed(unsigned char* dst, const float* src, int R, int K) {
+    for (int i = threadIdx.x; i < R * K; i += blockDim.x) {
+        int r = i / K, k = i % K;
+        put_bf16(dst, tc::kmajor_offset(k, r, R), src[i]);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_mlp_grad(int R, const float* __restrict__ X, const float* __restrict__ target,
+                                                  float scale, const float* __restrict__ P, float* __restrict__ G,
+                                                  float* __restrict__ loss_out, int* __restrict__ err) {
+    extern __shared__ __align__(1024) unsigned char s_raw[];
+    MlpGradSmem& S = *reinterpret_cast<MlpGradSmem*>(s_raw);
+    using namespace mlp;
+    int tid = threadIdx.x, warp = tid >> 5;
+    stage_matrix(S.w1, P + oW1, kHid, kIn);
+    stage_matrix(S.w2, P + oW2, kHid, kHid);
+    stage_matrix(S.w3, P + oW3, kHid, kHid);
+    stage_matrix(S.w4, P + oW4, kOut, kHid);
+    stage_transposed(S.w2t, P + oW2, kHid, kHid);
+    stage_transposed(S.w3t, P + oW3, kHid, kHid);
+    stage_transposed(S.w4t, P + oW4, kOut, kHid);
+    for (int i = tid; i < 3 * kHid + kOut; i += 128) {
+        S.bias[i] = P[oB1 + (i < kHid ? i : i < 2 * kHid ? (oB2 - oB1) + i - kHid
+                                              : i < 3 * kHid ? (oB3 - oB1) + i - 2 * kHid : (oB4 - oB1) + i - 3 * kHid)];
+        S.dbias[i] = 0.0f;
+    }
+    // dz4 columns 2..15 stay zero
+    for (int i = tid; i < kTile * kOut * 2 / 16; i += 128) reinterpret_cast<uint4*>(S.dz4)[i] = make_uint4(0, 0, 0, 0);
+    if (tid == 0) {
+        S.loss = 0.0f;
+        tc::mbar_init(&S.mbar, 1);
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(&S.taddr, 64);
+        tc::tmem_relinquish();
+    }
+    tc::fence_before_sync();
+    tc::fence_async_smem();
+    __syncthreads();
+    tc::fence_after_sync();
+    uint32_t taddr = S.taddr;
+    uint32_t lane_base = taddr + ((uint32_t)(warp * 32) << 16);
+    uint32_t phase = 0;
+    bool ok = true;
+    // register accumulators of the weight gradients:
+    //  W3, W2: thread t owns output o = t / 2, inputs (t % 2) * 32 .. +32
+    //  W1: output o = t / 2, inputs (t % 2) * 8 .. +8
+    //  W4: output row t / 64 (0 or 1), input t % 64
+    float g3[32], g2[32], g1[8], g4 = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 32; ++i) { g3[i] = 0.0f; g2[i] = 0.0f; }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) g1[i] = 0.0f;
+    const int go = tid >> 1, gi = (tid & 1) * 32, gi1 = (tid & 1) * 8;
+    float lsum = 0.0f;
+    int tiles = (R + kTile - 1) / kTile;
+    for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
+        int row = t * kTile + tid;
+        bool valid = row < R;
+#pragma unroll
+        for (int k = 0; k < kIn; ++k)
+            put_bf16(S.x, tc::kmajor_offset(tid, k, kIn), valid ? X[(size_t)row * kIn + k] : 0.0f);
+        tc::fence_async_smem();
+        __syncthreads();
+        // ---- forward
+        const unsigned char* a = S.x;
+        int K = kIn;
+        const unsigned char* ws[3] = {S.w1, S.w2, S.w3};
+        for (int l = 0; l < 3 && ok; ++l) {
+            ok = mlp_layer(taddr, a, ws[l], K, kHid, &S.mbar, phase);
+            if (!ok) break;
+            for (int c0 = 0; c0 < kHid; c0 += 16) {
+                float v[16];
+                tc::tmem_ld16(lane_base + (uint32_t)c0, v);
+#pragma unroll
+                for (int c = 0; c < 16; ++c)
+                    put_bf16(S.h[l], tc::kmajor_offset(tid, c0 + c, kHid),
+                             fmaxf(v[c] + S.bias[l * kHid + c0 + c], 0.0f));
+            }
+            tc::fence_before_sync();
+            tc::fence_async_smem();
+            __syncthreads();
+            a = S.h[l];
+            K = kHid;
+        }
+        if (!ok) break;
+        ok = mlp_layer(taddr, S.h[2], S.w4, kHid, kOut, &S.mbar, phase);
+        if (!ok) break;
+        {
+            float v[16];
+            tc::tmem_ld16(lane_base, v);
+            float z0 = v[0] + S.bias[3 * kHid], z1 = v[1] + S.bias[3 * kHid + 1];
+            float m = fmaxf(z0, z1);
+            float e0 = __expf(z0 - m), e1 = __expf(z1 - m);
+            float q0 = e0 / (e0 + e1);
+            float p = valid ? target[row] : 0.0f;
+            float d0 = valid ? (q0 - p) * scale : 0.0f;
+            if (valid) {
+                float lz = m + __logf(e0 + e1);
+                lsum += -(p * (z0 - lz) + (1.0f - p) * (z1 - lz));
+            }
+            S.dz4f[tid][0] = d0;
+            S.dz4f[tid][1] = -d0;
+            put_bf16(S.dz4, tc::kmajor_offset(tid, 0, kOut), d0);
+            put_bf16(S.dz4, tc::kmajor_offset(tid, 1, kOut), -d0);
+        }
+        tc::fence_before_sync();
+        tc::fence_async_smem();
+        __syncthreads();
+        // ---- backward, layer 4: dH3 = dZ4 * W4 (tensor cores), dW4, db4
+        ok = mlp_layer(taddr, S.dz4, S.w4t, kOut, kHid, &S.mbar, phase);
+        if (!ok) break;
+        {
+            int o4 = tid >> 6, i4 = tid & 63;
+            for (int r = 0; r < kTile; ++r)
+                g4 = fmaf(S.dz4f[r][o4], get_bf16(S.h[2], tc::kmajor_offset(r, i4, kHid)), g4);
+            if (tid < 2) {
+                float sb = 0.0f;
+                for (int r = 0; r < kTile; ++r) sb += S.dz4f[r][tid];
+                S.dbias[3 * kHid + tid] += sb;
+            }
+        }
+        // dZ3 = dH3 * relu'(Z3) -> dz[0]
+        for (int c0 = 0; c0 < kHid; c0 += 16) {
+            float v[16];
+            tc::tmem_ld16(lane_base + (uint32_t)c0, v);
+#pragma unroll
+            for (int c = 0; c < 16; ++c) {
+                float hv = get_bf16(S.h[2], tc::kmajor_offset(tid, c0 + c, kHid));
+                put_bf16(S.dz[0], tc::kmajor_offset(tid, c0 + c, kHid), hv > 0.0f ? v[c] : 0.0f);
+            }
+        }
+        tc::fence_before_sync();
+        tc::fence_async_smem();
+        __syncthreads();
+        // layers 3 and 2: dH_{l-1} = dZ_l * W_l on the tensor cores while the
+        // CUDA cores reduce dW_l = dZ_l^T H_{l-1}
+        const unsigned char* wt[2] = {S.w3t, S.w2t};
+        float* gacc[2] = {g3, g2};
+        for (int l = 0; l < 2 && ok; ++l) {
+            const unsigned char* dzl = S.dz[l];
+            const unsigned char* hprev = S.h[1 - l];  // H2 for layer 3, H1 for layer 2
+            if (tid == 0) {
+                tc::fence_after_sync();
+                uint32_t idesc = tc::idesc_bf16(128, kHid);
+                for (int ks = 0; ks < kHid / 16; ++ks)
+                    tc::mma_bf16(taddr, tc::smem_desc(tc::smem_u32(dzl) + ks * 256, 128, 8 * 128),
+                                 tc::smem_desc(tc::smem_u32(wt[l]) + ks * 256, 128, 8 * 128), idesc, ks > 0);
+                tc::mma_commit(&S.mbar);
+            }
+            float* gg = gacc[l];
+            for (int r = 0; r < kTile; ++r) {
+                float dzv = get_bf16(dzl, tc::kmajor_offset(r, go, kHid));
+#pragma unroll
+                for (int c8 = 0; c8 < 4; ++c8) {
+                    float hv[8];
+                    get8(hprev, r, gi + 8 * c8, kHid, hv);
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) gg[8 * c8 + q] = fmaf(dzv, hv[q], gg[8 * c8 + q]);
+                }
+            }
+            if (tid < kHid) {
+                float sb = 0.0f;
+                for (int r = 0; r < kTile; ++r) sb += get_bf16(dzl, tc::kmajor_offset(r, tid, kHid));
+                S.dbias[(2 - l) * kHid + tid] += sb;
+            }
+            ok = tc::mbar_wait(&S.mbar, phase & 1u, kWaitLimit);
+            ++phase;
+            tc::fence_after_sync();
+            ok = __syncthreads_and(ok) != 0;
+            if (!ok) break;
+            // dZ_{l-1} = dH * relu'(Z_{l-1}) -> the other dz buffer
+            unsigned char* dzn = S.dz[1 - l];
+            for (int c0 = 0; c0 < kHid; c0 += 16) {
+                float v[16];
+                tc::tmem_ld16(lane_base + (uint32_t)c0, v);
+#pragma unroll
+                for (int c = 0; c < 16; ++c) {
+                    float hv = get_bf16(hprev, tc::kmajor_offset(tid, c0 + c, kHid));
+                    put_bf16(dzn, tc::kmajor_offset(tid, c0 + c, kHid), hv > 0.0f ? v[c] : 0.0f);
+                }
+            }
+            tc::fence_before_sync();
+            tc::fence_async_smem();
+            __syncthreads();
+        }
+        if (!ok) break;
+        // layer 1: dW1 = dZ1^T X, db1 (dZ1 is in dz[0] after two swaps)
+        {
+            const unsigned char* dz1 = S.dz[0];
+            for (int r = 0; r < kTile; ++r) {
+                float dzv = get_bf16(dz1, tc::kmajor_offset(r, go, kHid));
+                float xv[8];
+                get8(S.x, r, gi1, kIn, xv);
+#pragma unroll
+                for (int q = 0; q < 8; ++q) g1[q] = fmaf(dzv, xv[q], g1[q]);
+            }
+            if (tid < kHid) {
+                float sb = 0.0f;
+                for (int r = 0; r < kTile; ++r) sb += get_bf16(dz1, tc::kmajor_offset(r, tid, kHid));
+                S.dbias[tid] += sb;
+            }
+        }
+        __syncthreads();
+    }
+    if (!ok && (tid & 31) == 0) atomicExch(err, 1);
+    // flush the accumulators
+#pragma unroll
+    for (int i = 0; i < 32; ++i) {
+        atomicAdd(&G[oW3 + go * kHid + gi + i], g3[i]);
+        atomicAdd(&G[oW2 + go * kHid + gi + i], g2[i]);
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) atomicAdd(&G[oW1 + go * kIn + gi1 + i], g1[i]);
+    atomicAdd(&G[oW4 + (tid >> 6) * kHid + (tid & 63)], g4);
+    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+    if ((tid & 31) == 0) atomicAdd(&S.loss, lsum);
+    tc::fence_before_sync();
+    __syncthreads();
+    for (int i = tid; i < kHid; i += 128) {
+        atomicAdd(&G[oB1 + i], S.dbias[i]);
+        atomicAdd(&G[oB2 + i], S.dbias[kHid + i]);
+        atomicAdd(&G[oB3 + i], S.dbias[2 * kHid + i]);
+    }
+    if (tid < 2) atomicAdd(&G[oB4 + tid], S.dbias[3 * kHid + tid]);
+    if (tid == 0) atomicAdd(loss_out, S.loss * scale);
+    if (warp == 0) tc::tmem_dealloc(taddr, 64);
+}
+
+// Adam step on the flat parameters; the gradient is consumed (zeroed).
+// Rows 2..15 of W4 and entries 2..15 of b4 stay zero.
+__global__ void k_mlp_adam(float* __restrict__ P, float* __restrict__ G, float* __restrict__ M1,
+                           float* __restrict__ M2, float lr, float beta1, float beta2, float eps, float c1,
+                           float c2) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= mlp::kParams) return;
+    bool dead = (i >= mlp::oW4 + 2 * mlp::kHid && i < mlp::oB4) || i >= mlp::oB4 + 2;
+    float g = G[i];
+    G[i] = 0.0f;
+    if (dead) return;
+    float m = beta1 * M1[i] + (1.0f - beta1) * g;
+    float v = beta2 * M2[i] + (1.0f - beta2) * g * g;
+    M1[i] = m;
+    M2[i] = v;
+    P[i] -= lr * (m / c1) / (sqrtf(v / c2) + eps);
+}
+
 }  // namespace uds
 
 extern "C" int uds_mlp_param_count(void) { return uds::mlp::kParams; }
@@ -248,5 +541,35 @@ extern "C" int uds_mlp_forward(int R, const float* X, const float* params, float
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int grid = tiles < 4 * sms ? tiles : 4 * sms;
     k_mlp_forward<<<grid, 128, smem, as_stream(stream)>>>(R, X, params, logits, err);
+    return launch_status();
+}
+
+extern "C" int uds_mlp_grad(int R, const float* X, const float* target, const float* params, float* grad,
+                            float* loss, int* err, void* stream) {
+    using namespace uds;
+    if (R < 0 || (R > 0 && (!X || !target || !params || !grad || !loss)) || !err) return UDS_ERR_ARGUMENT;
+    if (R == 0) return UDS_OK;
+    static bool attr = false;
+    size_t smem = sizeof(MlpGradSmem) + 1024;
+    if (!attr) {
+        cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr = true;
+    }
+    int tiles = (R + mlp::kTile - 1) / mlp::kTile;
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int grid = tiles < sms ? tiles : sms;
+    k_mlp_grad<<<grid, 128, smem, as_stream(stream)>>>(R, X, target, 1.0f / (float)R, params, grad, loss, err);
+    return launch_status();
+}
+
+extern "C" int uds_mlp_adam(float* params, float* grad, float* m1, float* m2, int step, float lr, float beta1,
+                            float beta2, float eps, void* stream) {
+    using namespace uds;
+    if (!params || !grad || !m1 || !m2 || step < 1) return UDS_ERR_ARGUMENT;
+    float c1 = 1.0f - powf(beta1, (float)step), c2 = 1.0f - powf(beta2, (float)step);
+    k_mlp_adam<<<cdiv(mlp::kParams, 256), 256, 0, as_stream(stream)>>>(params, grad, m1, m2, lr, beta1, beta2, eps,
+                                                                      c1, c2);
     return launch_status();
 }
