@@ -107,6 +107,31 @@ int uds_sample_stochastic(const uds_sample_params* prm, const float* points, con
                           const float* std_devs, const float* h_override, int32_t* indices, float* probs,
                           uds_view_stats* stats, void* workspace, size_t workspace_bytes, void* stream);
 
+/* Learned-proposal sampling (no counterpart in the reference): K weighted
+ * draws per pixel.  With mlp_params (uds_mlp_param_count() floats) each draw
+ * descends by the network's branch probabilities q (16 features per node,
+ * evaluated level by level on the tensor cores) and gets the importance
+ * weight (leaf Gaussian / root FGT mass) / q_path, an unbiased estimator for
+ * any q > 0.  Pixels whose effective sample size (sum w)^2 / sum w^2 is below
+ * ess_tau * K are redrawn by the stochastic sampler (their weights then use
+ * its exact path probabilities); fallback (B,W,H) uint8 and n_fallback[B]
+ * report them (either may be NULL).  With mlp_params NULL every pixel uses
+ * the stochastic sampler.  indices (B,W,H,K) int32 (-1: none), weights
+ * (B,W,H,K) float32.  Workspace: uds_proposal_workspace_size. */
+size_t uds_proposal_workspace_size(const uds_sample_params* prm);
+int uds_sample_proposal(const uds_sample_params* prm, const float* points, const float* normals,
+                        const float* std_devs, const float* h_override, const float* mlp_params, float ess_tau,
+                        int32_t* indices, float* weights, uint8_t* fallback, int32_t* n_fallback,
+                        uds_view_stats* stats, void* workspace, size_t workspace_bytes, void* stream);
+/* Training rows for the proposal network from the tree already built by
+ * uds_tree_build in `workspace`: stochastic descents with exact FGT masses
+ * from every stride-th pixel (both directions), `draws` per pixel; each
+ * visited internal node appends (16 features, m_left / (m_left + m_right)) to
+ * X (cap x 16) and target (cap).  *count (device int, preset to 0) receives
+ * the number of rows produced (it may exceed cap; rows past cap are dropped). */
+int uds_proposal_dataset(const uds_sample_params* prm, int stride, int draws, float* X, float* target,
+                         int32_t* count, int cap, const void* workspace, size_t workspace_bytes, void* stream);
+
 /* Debug view of one tree (for tests): builds view `view` and copies the
  * first n_visible entries of each array (host-sized by the caller from
  * stats).  Any output pointer may be NULL.  Arrays: keys/ids (n), node arrays
@@ -143,6 +168,9 @@ int uds_mma_probe(int N, int K, const uint16_t* A, const uint16_t* B, float* C, 
  * with fp32 accumulation.  uds_mlp_forward: X (R x 16) -> logits (R x 2). */
 int uds_mlp_param_count(void);
 int uds_mlp_forward(int R, const float* X, const float* params, float* logits, int* err, void* stream);
+/* Same, the row count read on the device from *R_dev (at most R_max rows). */
+int uds_mlp_forward_dev(int R_max, const int* R_dev, const float* X, const float* params, float* logits, int* err,
+                        void* stream);
 /* Training: adds the gradient of the mean cross-entropy between
  * softmax(logits) and (target, 1 - target) over the R rows to grad (fp32,
  * uds_mlp_param_count() entries, zeroed by the caller) and the mean loss to

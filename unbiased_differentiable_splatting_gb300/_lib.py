@@ -59,6 +59,13 @@ _SIGS = {
     "uds_mlp_grad": (c_int, [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "uds_mlp_adam": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_float, c_float, c_float, c_float,
                              c_void_p]),
+    "uds_mlp_forward_dev": (c_int, [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "uds_proposal_workspace_size": (c_size_t, [ctypes.POINTER(SampleParams)]),
+    "uds_sample_proposal": (c_int, [ctypes.POINTER(SampleParams), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                    c_float, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
+                                    c_void_p]),
+    "uds_proposal_dataset": (c_int, [ctypes.POINTER(SampleParams), c_int, c_int, c_void_p, c_void_p, c_void_p, c_int,
+                                     c_void_p, c_size_t, c_void_p]),
     "uds_splat_workspace_size": (c_size_t, [c_int, c_int]),
     "uds_splat_forward": (c_int, [c_int, c_int, c_int, c_int, c_float, c_void_p, c_void_p, c_void_p, c_int,
                                   c_int, c_void_p, c_float, c_void_p, c_void_p, c_size_t, c_void_p]),

@@ -151,9 +151,11 @@ __device__ __forceinline__ bool mlp_layer(uint32_t taddr, const unsigned char* a
 
 // Inference: logits (R x 2, fp32) of feature rows X (R x 16, fp32).
 // Persistent CTAs of 128 threads; thread t owns row t of each 128-row tile.
-__global__ void __launch_bounds__(128) k_mlp_forward(int R, const float* __restrict__ X,
+__global__ void __launch_bounds__(128) k_mlp_forward(int R, const int* __restrict__ Rdev, const float* __restrict__ X,
                                                      const float* __restrict__ P, float* __restrict__ out,
                                                      int* __restrict__ err) {
+    if (Rdev) R = min(R, *Rdev);  // row count produced on the device
+    if ((int)blockIdx.x * mlp::kTile >= R) return;  // no tile for this CTA
     extern __shared__ __align__(1024) unsigned char s_raw[];
     MlpFwdSmem& S = *reinterpret_cast<MlpFwdSmem*>(s_raw);
     using namespace mlp;
@@ -540,7 +542,28 @@ extern "C" int uds_mlp_forward(int R, const float* X, const float* params, float
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int grid = tiles < 4 * sms ? tiles : 4 * sms;
-    k_mlp_forward<<<grid, 128, smem, as_stream(stream)>>>(R, X, params, logits, err);
+    k_mlp_forward<<<grid, 128, smem, as_stream(stream)>>>(R, nullptr, X, params, logits, err);
+    return launch_status();
+}
+
+// Same, with the row count read on the device from *R_dev (at most R_max).
+extern "C" int uds_mlp_forward_dev(int R_max, const int* R_dev, const float* X, const float* params, float* logits,
+                                   int* err, void* stream) {
+    using namespace uds;
+    if (R_max < 0 || !R_dev || (R_max > 0 && (!X || !params || !logits)) || !err) return UDS_ERR_ARGUMENT;
+    if (R_max == 0) return UDS_OK;
+    static bool attr = false;
+    size_t smem = sizeof(MlpFwdSmem) + 1024;
+    if (!attr) {
+        cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr = true;
+    }
+    int tiles = (R_max + mlp::kTile - 1) / mlp::kTile;
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int grid = tiles < 4 * sms ? tiles : 4 * sms;
+    k_mlp_forward<<<grid, 128, smem, as_stream(stream)>>>(R_max, R_dev, X, params, logits, err);
     return launch_status();
 }
 

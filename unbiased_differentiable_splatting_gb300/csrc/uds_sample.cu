@@ -1060,7 +1060,8 @@ __global__ void __launch_bounds__(128) k_stochastic(Tree T, const ViewState* vs,
                                                     float precision, uint64_t seed,
                                                     const uint64_t* __restrict__ seed_ptr, uint32_t view,
                                                     int* __restrict__ indices, float* __restrict__ probs,
-                                                    uds_view_stats* st) {
+                                                    uds_view_stats* st, const unsigned char* __restrict__ mask,
+                                                    float* __restrict__ weights) {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     int i = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= W || j >= H) return;
@@ -1070,8 +1071,10 @@ __global__ void __launch_bounds__(128) k_stochastic(Tree T, const ViewState* vs,
     int n = T.n;
     if (n == 0) return;
     size_t pixel = (size_t)j + (size_t)H * i;
+    if (mask && !mask[pixel]) return;
     float qx = (float)i, qy = (float)j;
-    if (fmaxf(0.0f, node_weight(T, 0, qx, qy)) < precision) return;
+    float m0 = fmaxf(0.0f, node_weight(T, 0, qx, qy));
+    if (m0 < precision) return;
     int cn[kTrace];
     float cm0[kTrace], cm1[kTrace];
     for (int d = 0; d < kTrace; ++d) cn[d] = -1;
@@ -1112,9 +1115,229 @@ __global__ void __launch_bounds__(128) k_stochastic(Tree T, const ViewState* vs,
         if (ok) {
             out[k] = T.leaf_id[v - (n - 1)];
             pq[k] = prob;
+            // importance weight of the draw: (leaf mass / root mass) / q
+            if (weights) weights[(size_t)K * pixel + k] = hermite_eval(T, v, T.cen[v], qx, qy) / m0 / prob;
         }
     }
     if (overflow) atomicAdd(&st->overflow, 1);
+}
+
+// ============================================================ proposal
+// Learned proposal for the stochastic mode (no reference counterpart).  A
+// draw descends from the root; at each internal node a small network maps
+// 16 cheap features of the node's two children (offsets of the query from
+// their centres, their leaf counts, box distances and sizes, all in units of
+// sqrt(2) h) to the probability q of the left branch, instead of evaluating
+// both children's FGT masses.  The draw's importance weight is
+// p / q_path with p = (leaf Gaussian) / (root FGT mass): only the root mass
+// is evaluated per pixel, and the weighted estimator stays unbiased because
+// q > 0 on every branch.  The descent runs level-synchronously over all
+// draws so that each level's network evaluations form one batch for the
+// tensor-core kernel (uds_mlp_forward_dev).
+constexpr int kFeat = 16;
+
+__device__ __forceinline__ float feat_clamp(float x) { return fminf(fmaxf(x, -16.0f), 16.0f); }
+
+__device__ __forceinline__ float box_distance(float4 b, float qx, float qy) {
+    float dx = fmaxf(fmaxf(b.x - qx, qx - b.z), 0.0f), dy = fmaxf(fmaxf(b.y - qy, qy - b.w), 0.0f);
+    return sqrtf(dx * dx + dy * dy);
+}
+
+__device__ void branch_features(const Tree& T, int v, int depth, float qx, float qy, float* f) {
+    int4 L = T.lnk[v];
+    float is = 1.0f / T.sq;
+    float bd[2];
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+        int x = c ? L.y : L.x;
+        float4 cc = T.cen[x], b = T.box[x];
+        int cnt = T.lnk[x].w;
+        bd[c] = box_distance(b, qx, qy) * is;
+        f[6 * c + 0] = feat_clamp((qx - cc.x) * is);
+        f[6 * c + 1] = feat_clamp((qy - cc.y) * is);
+        f[6 * c + 2] = log2f((float)cnt) * 0.125f;
+        f[6 * c + 3] = feat_clamp(bd[c]);
+        f[6 * c + 4] = feat_clamp(0.5f * sqrtf((b.z - b.x) * (b.z - b.x) + (b.w - b.y) * (b.w - b.y)) * is);
+        f[6 * c + 5] = x >= T.n - 1 ? 1.0f : 0.0f;
+    }
+    f[12] = (float)depth * (1.0f / 32.0f);
+    f[13] = log2f((float)L.w) * 0.125f;
+    f[14] = feat_clamp(bd[0] - bd[1]);
+    f[15] = 0.0f;
+}
+
+__device__ __forceinline__ float draw_uniform(uint64_t seed, uint32_t pixel, uint32_t view, uint32_t tag, int k,
+                                              int level) {
+    uint32_t c[4] = {pixel, view, tag | ((uint32_t)k << 8) | (uint32_t)(level >> 2), 0u};
+    philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+    return bits_to_uniform(c[level & 3]);
+}
+
+// Training rows: plain stochastic descents (exact FGT masses) from every
+// stride-th pixel in each direction, `draws` per pixel; each internal node
+// visited gives (features, m_left / (m_left + m_right)).
+__global__ void __launch_bounds__(128) k_prop_dataset(Tree T, const ViewState* vs, int W, int H, int stride,
+                                                      int draws, float precision, uint64_t seed, uint32_t view,
+                                                      float* __restrict__ X, float* __restrict__ target,
+                                                      int* __restrict__ count, int cap) {
+    int j = (blockIdx.x * blockDim.x + threadIdx.x) * stride;
+    int i = (blockIdx.y * blockDim.y + threadIdx.y) * stride;
+    if (i >= W || j >= H) return;
+    T.n = vs->n;
+    T.sq = vs->sq;
+    int n = T.n;
+    if (n < 2) return;
+    float qx = (float)i, qy = (float)j;
+    if (fmaxf(0.0f, node_weight(T, 0, qx, qy)) < precision) return;
+    uint32_t pixel = (uint32_t)(j + H * i);
+    int cn[kTrace];
+    float cm0[kTrace], cm1[kTrace];
+    for (int d = 0; d < kTrace; ++d) cn[d] = -1;
+    for (int k = 0; k < draws; ++k) {
+        int v = 0;
+        for (int d = 0; v < n - 1 && d < kTrace; ++d) {
+            int4 L = T.lnk[v];
+            float w0, w1;
+            if (cn[d] == v) {
+                w0 = cm0[d];
+                w1 = cm1[d];
+            } else {
+                w0 = fmaxf(0.0f, node_weight(T, L.x, qx, qy));
+                w1 = fmaxf(0.0f, node_weight(T, L.y, qx, qy));
+                cn[d] = v;
+                cm0[d] = w0;
+                cm1[d] = w1;
+            }
+            float sum = w0 + w1;
+            if (!(sum > 0.0f)) break;
+            float pl = w0 / sum;
+            int r = atomicAdd(count, 1);
+            if (r < cap) {
+                float f[kFeat];
+                branch_features(T, v, d, qx, qy, f);
+#pragma unroll
+                for (int q = 0; q < kFeat; ++q) X[(size_t)r * kFeat + q] = f[q];
+                target[r] = pl;
+            }
+            v = draw_uniform(seed, pixel, view, 0xA0000000u, k, d) <= pl ? L.x : L.y;
+        }
+    }
+}
+
+// Per pixel: root mass; active pixels put their K draws on the list.
+__global__ void k_prop_init(Tree T, const ViewState* vs, int W, int H, int K, float precision,
+                            float* __restrict__ root_mass, int* __restrict__ node_out, int* __restrict__ draw_out,
+                            float* __restrict__ logq_out, int* __restrict__ count_out, int* __restrict__ indices,
+                            float* __restrict__ weights) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    int i = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= W || j >= H) return;
+    T.n = vs->n;
+    T.sq = vs->sq;
+    size_t pixel = (size_t)j + (size_t)H * i;
+    float qx = (float)i, qy = (float)j;
+    float m0 = T.n > 0 ? fmaxf(0.0f, node_weight(T, 0, qx, qy)) : 0.0f;
+    root_mass[pixel] = m0;
+    if (T.n == 0 || m0 < precision) return;
+    if (T.n == 1) {  // the root is the only leaf
+        for (int k = 0; k < K; ++k) {
+            indices[(size_t)K * pixel + k] = T.leaf_id[0];
+            weights[(size_t)K * pixel + k] = hermite_eval(T, 0, T.cen[0], qx, qy) / m0;
+        }
+        return;
+    }
+    int base = atomicAdd(count_out, K);
+    for (int k = 0; k < K; ++k) {
+        node_out[base + k] = 0;
+        draw_out[base + k] = (int)(pixel * K + k);
+        logq_out[base + k] = 0.0f;
+    }
+}
+
+__global__ void k_prop_features(Tree T, const ViewState* vs, int H, int K, int level, const int* __restrict__ count,
+                                const int* __restrict__ node_in, const int* __restrict__ draw_in,
+                                float* __restrict__ X) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= *count) return;
+    T.n = vs->n;
+    T.sq = vs->sq;
+    int pixel = draw_in[r] / K;
+    float qx = (float)(pixel / H), qy = (float)(pixel % H);
+    float f[kFeat];
+    branch_features(T, node_in[r], level, qx, qy, f);
+#pragma unroll
+    for (int q = 0; q < kFeat; ++q) X[(size_t)r * kFeat + q] = f[q];
+}
+
+// Take one branch per draw with the network's q; finished draws write their
+// leaf and importance weight, the others go on the next level's list.
+__global__ void k_prop_step(Tree T, const ViewState* vs, int H, int K, int level, uint64_t seed,
+                            const uint64_t* __restrict__ seed_ptr, uint32_t view, const int* __restrict__ count_in,
+                            const int* __restrict__ node_in, const int* __restrict__ draw_in,
+                            const float* __restrict__ logq_in, const float* __restrict__ logits,
+                            const float* __restrict__ root_mass, int* __restrict__ count_out,
+                            int* __restrict__ node_out, int* __restrict__ draw_out, float* __restrict__ logq_out,
+                            int* __restrict__ indices, float* __restrict__ weights) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= *count_in) return;
+    if (seed_ptr) seed = *seed_ptr;
+    T.n = vs->n;
+    T.sq = vs->sq;
+    int draw = draw_in[r];
+    int pixel = draw / K, k = draw % K;
+    int v = node_in[r];
+    int4 L = T.lnk[v];
+    float z0 = logits[2 * r], z1 = logits[2 * r + 1];
+    float m = fmaxf(z0, z1);
+    float e0 = __expf(z0 - m), e1 = __expf(z1 - m);
+    float q0 = e0 / (e0 + e1);
+    float u = draw_uniform(seed, (uint32_t)pixel, view, 0xC0000000u, k, level);
+    bool left = u <= q0;
+    float qc = left ? q0 : 1.0f - q0;
+    float logq = logq_in[r] + __logf(fmaxf(qc, 1e-30f));
+    int c = left ? L.x : L.y;
+    if (c >= T.n - 1) {
+        float qx = (float)(pixel / H), qy = (float)(pixel % H);
+        float g = hermite_eval(T, c, T.cen[c], qx, qy);
+        indices[draw] = T.leaf_id[c - (T.n - 1)];
+        weights[draw] = g / root_mass[pixel] * __expf(-logq);
+    } else if (level + 1 < kTrace) {
+        int o = atomicAdd(count_out, 1);
+        node_out[o] = c;
+        draw_out[o] = draw;
+        logq_out[o] = logq;
+    }
+}
+
+// Effective sample size of each pixel's K weighted draws; pixels below
+// tau * K are marked for the plain sampler.
+__global__ void k_prop_ess(int W, int H, int K, float tau, const float* __restrict__ root_mass, float precision,
+                           const float* __restrict__ weights, unsigned char* __restrict__ mask,
+                           int* __restrict__ nfallback) {
+    size_t pixel = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (pixel >= (size_t)W * H) return;
+    unsigned char fb = 0;
+    if (root_mass[pixel] >= precision) {
+        float s1 = 0.0f, s2 = 0.0f;
+        for (int k = 0; k < K; ++k) {
+            float w = weights[(size_t)K * pixel + k];
+            s1 += w;
+            s2 += w * w;
+        }
+        fb = !(s2 > 0.0f && s1 * s1 >= tau * (float)K * s2);  // also when no draw finished
+    }
+    mask[pixel] = fb;
+    if (fb) atomicAdd(nfallback, 1);
+}
+
+__global__ void k_prop_clear(size_t P, int K, const unsigned char* __restrict__ mask, int* __restrict__ indices,
+                             float* __restrict__ weights) {
+    size_t pixel = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (pixel >= P || !mask[pixel]) return;
+    for (int k = 0; k < K; ++k) {
+        indices[(size_t)K * pixel + k] = -1;
+        weights[(size_t)K * pixel + k] = 0.0f;
+    }
 }
 
 __global__ void k_finish_view(const ViewState* vs, uds_view_stats* st) {
@@ -1312,7 +1535,7 @@ extern "C" int uds_sample_stochastic(const uds_sample_params* prm, const float* 
         if ((st = build_view(prm, w, b, points, normals, std_devs, h_override, s))) return st;
         if (prm->N == 0) continue;
         k_stochastic<<<grid, block, 0, s>>>(T, w.vs, prm->W, prm->H, prm->K, prm->precision, prm->seed, prm->seed_dev, (uint32_t)b,
-                                            indices + per_view * b, probs + per_view * b, w.stats + b);
+                                            indices + per_view * b, probs + per_view * b, w.stats + b, nullptr, nullptr);
         if ((st = launch_status())) return st;
     }
     if (stats) {
@@ -1408,5 +1631,140 @@ extern "C" int uds_fgt_eval(const uds_sample_params* prm, int m, const int32_t* 
     if (!workspace || workspace_bytes < w.bytes) return UDS_ERR_WORKSPACE;
     if (m <= 0) return UDS_OK;
     k_fgt_eval<<<cdiv(m, 128), 128, 0, as_stream(stream)>>>(tree_of(w), w.vs, m, nodes, query_xy, out);
+    return launch_status();
+}
+
+extern "C" int uds_mlp_forward_dev(int R_max, const int* R_dev, const float* X, const float* params, float* logits,
+                                   int* err, void* stream);
+
+namespace uds {
+// Proposal-mode buffers after the tree slot.
+struct PropWs {
+    float* root_mass;
+    unsigned char* mask;
+    int* node[2];
+    int* draw[2];
+    float* logq[2];
+    float* X;
+    float* logits;
+    int* counts;  // [0], [1]: list lengths; [2]: fallback pixels; [3]: network error flag
+    size_t bytes;
+};
+
+static PropWs prop_layout(const uds_sample_params* p, char* base) {
+    PropWs q{};
+    size_t P = (size_t)p->W * p->H, D = P * (size_t)p->K;
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off += a256(bytes); return base ? base + o : nullptr; };
+    q.root_mass = (float*)take(4 * P);
+    q.mask = (unsigned char*)take(P);
+    for (int c = 0; c < 2; ++c) {
+        q.node[c] = (int*)take(4 * D);
+        q.draw[c] = (int*)take(4 * D);
+        q.logq[c] = (float*)take(4 * D);
+    }
+    q.X = (float*)take(4 * kFeat * D);
+    q.logits = (float*)take(8 * D);
+    q.counts = (int*)take(16);
+    q.bytes = off;
+    return q;
+}
+}  // namespace uds
+
+extern "C" size_t uds_proposal_workspace_size(const uds_sample_params* prm) {
+    if (check_params(prm)) return 0;
+    return layout(prm, nullptr).bytes + prop_layout(prm, nullptr).bytes;
+}
+
+extern "C" int uds_sample_proposal(const uds_sample_params* prm, const float* points, const float* normals,
+                                   const float* std_devs, const float* h_override, const float* mlp_params,
+                                   float ess_tau, int32_t* indices, float* weights, uint8_t* fallback,
+                                   int32_t* n_fallback, uds_view_stats* stats, void* workspace,
+                                   size_t workspace_bytes, void* stream) {
+    int st = check_params(prm);
+    if (st) return st;
+    if (!indices || !weights || (prm->N > 0 && (!points || !normals || !std_devs))) return UDS_ERR_ARGUMENT;
+    if (prm->W * (size_t)prm->H * prm->K >= (1ull << 31)) return UDS_ERR_ARGUMENT;
+    char* base = reinterpret_cast<char*>(workspace);
+    Ws w = layout(prm, base);
+    PropWs q = prop_layout(prm, base ? base + w.bytes : nullptr);
+    if (!workspace || workspace_bytes < w.bytes + q.bytes) return UDS_ERR_WORKSPACE;
+    cudaStream_t s = as_stream(stream);
+    size_t P = (size_t)prm->W * prm->H, per_view = P * prm->K;
+    cudaError_t e = cudaMemsetAsync(indices, 0xFF, sizeof(int32_t) * per_view * prm->B, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(weights, 0, sizeof(float) * per_view * prm->B, s);
+    if (e == cudaSuccess && n_fallback) e = cudaMemsetAsync(n_fallback, 0, sizeof(int32_t) * prm->B, s);
+    if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
+    Tree T = tree_of(w);
+    dim3 block(16, 8);
+    dim3 grid(cdiv(prm->H, block.x), cdiv(prm->W, block.y));
+    for (int b = 0; b < prm->B; ++b) {
+        if ((st = build_view(prm, w, b, points, normals, std_devs, h_override, s))) return st;
+        if (prm->N == 0) continue;
+        int* idx = indices + per_view * b;
+        float* wt = weights + per_view * b;
+        const unsigned char* mask = nullptr;
+        if (mlp_params) {
+            e = cudaMemsetAsync(q.counts, 0, 16, s);
+            if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
+            k_prop_init<<<grid, block, 0, s>>>(T, w.vs, prm->W, prm->H, prm->K, prm->precision, q.root_mass,
+                                               q.node[0], q.draw[0], q.logq[0], q.counts, idx, wt);
+            if ((st = launch_status())) return st;
+            unsigned nb = cdiv(per_view, 256);
+            int cur = 0;
+            for (int level = 0; level < kTrace; ++level) {
+                k_prop_features<<<nb, 256, 0, s>>>(T, w.vs, prm->H, prm->K, level, q.counts + cur, q.node[cur],
+                                                   q.draw[cur], q.X);
+                if ((st = launch_status())) return st;
+                if ((st = uds_mlp_forward_dev((int)per_view, q.counts + cur, q.X, mlp_params, q.logits, q.counts + 3,
+                                              stream)))
+                    return st;
+                e = cudaMemsetAsync(q.counts + (cur ^ 1), 0, 4, s);
+                if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
+                k_prop_step<<<nb, 256, 0, s>>>(T, w.vs, prm->H, prm->K, level, prm->seed, prm->seed_dev, (uint32_t)b,
+                                               q.counts + cur, q.node[cur], q.draw[cur], q.logq[cur], q.logits,
+                                               q.root_mass, q.counts + (cur ^ 1), q.node[cur ^ 1], q.draw[cur ^ 1],
+                                               q.logq[cur ^ 1], idx, wt);
+                if ((st = launch_status())) return st;
+                cur ^= 1;
+            }
+            k_prop_ess<<<cdiv(P, 256), 256, 0, s>>>(prm->W, prm->H, prm->K, ess_tau, q.root_mass, prm->precision, wt,
+                                                     q.mask, n_fallback ? n_fallback + b : q.counts + 2);
+            if ((st = launch_status())) return st;
+            // fallback pixels: clear the proposal's draws, then the plain sampler
+            k_prop_clear<<<cdiv(P, 256), 256, 0, s>>>(P, prm->K, q.mask, idx, wt);
+            if ((st = launch_status())) return st;
+            mask = q.mask;
+            if (fallback) {
+                e = cudaMemcpyAsync(fallback + P * b, q.mask, P, cudaMemcpyDeviceToDevice, s);
+                if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
+            }
+        }
+        // the plain stochastic sampler: every pixel, or the fallback pixels
+        float* probs = q.logits;  // scratch for the path probabilities
+        k_stochastic<<<grid, block, 0, s>>>(T, w.vs, prm->W, prm->H, prm->K, prm->precision, prm->seed,
+                                            prm->seed_dev, (uint32_t)b, idx, probs, w.stats + b, mask, wt);
+        if ((st = launch_status())) return st;
+    }
+    if (stats) {
+        e = cudaMemcpyAsync(stats, w.stats, sizeof(uds_view_stats) * prm->B, cudaMemcpyDeviceToDevice, s);
+        if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
+    }
+    return UDS_OK;
+}
+
+extern "C" int uds_proposal_dataset(const uds_sample_params* prm, int stride, int draws, float* X, float* target,
+                                    int32_t* count, int cap, const void* workspace, size_t workspace_bytes,
+                                    void* stream) {
+    int st = check_params(prm);
+    if (st) return st;
+    if (stride < 1 || draws < 1 || cap < 0 || !count || (cap > 0 && (!X || !target))) return UDS_ERR_ARGUMENT;
+    Ws w = layout(prm, reinterpret_cast<char*>(const_cast<void*>(workspace)));
+    if (!workspace || workspace_bytes < w.bytes) return UDS_ERR_WORKSPACE;
+    if (prm->N == 0) return UDS_OK;
+    dim3 block(16, 8);
+    dim3 grid(cdiv(cdiv(prm->H, stride), block.x), cdiv(cdiv(prm->W, stride), block.y));
+    k_prop_dataset<<<grid, block, 0, as_stream(stream)>>>(tree_of(w), w.vs, prm->W, prm->H, stride, draws,
+                                                          prm->precision, prm->seed, 0u, X, target, count, cap);
     return launch_status();
 }
