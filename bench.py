@@ -340,16 +340,110 @@ def multiview_main(args, name, wl):
         else None, "clocks": clk, "gpu_launches": int(launches)}), flush=True)
 
 
+def proposal_main(args):
+    """Learned proposal against the plain stochastic sampler on the 500k /
+    1024^2 / K=8 view: time per sampling call (CUDA events, device-resident
+    inputs), per-pixel variance of the weighted image estimate over seeds, and
+    the wall time the learned sampler needs to reach the plain sampler's
+    variance (variance scales as 1 / draws)."""
+    import torch
+    from unbiased_differentiable_splatting_gb300 import load, proposal, scenes
+    from unbiased_differentiable_splatting_gb300.extensions import transformForward, world2Camera
+    from unbiased_differentiable_splatting_gb300.cudaExtensions import transform
+    L = load()
+    dev = torch.device("cuda", 0)
+    wl = WORKLOADS["harmonic500k"]
+    sc = make_scene(wl)
+    W = H = wl["width"]
+    K, prec = wl["K"], wl["precision"]
+    d = {k: v.to(dev) for k, v in sc.items() if isinstance(v, torch.Tensor)}
+    with torch.no_grad():
+        M = transformForward(world2Camera(d["cam_positions"], d["cam_orientations"]), "-z").squeeze(1).contiguous()
+        cp = transform.affineForward(M, d["points"])
+        cn = transform.linearForward(M, d["normals"])
+        cnb = torch.where(cn[..., 2:] > 0, -cn, cn).contiguous()
+    args_ = (W, H, sc["focal"], cp, cnb, d["stddevs"])
+    values = d["colors"][..., :1].contiguous()
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(net, seeds):
+        out, ts = [], []
+        for s in seeds:
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            idx, w, fb, nfb = proposal.sample(*args_, K, 0.0, prec, net=net, ess_tau=0.1, seed=s)
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+            out.append((proposal.estimate(idx, w, values)[0, ..., 0], int(nfb.sum())))
+        return out, ts
+
+    # training: rows from the sampler itself, then Adam on the tensor cores
+    t0 = time.perf_counter()
+    X, tgt = proposal.dataset(*args_, 0.0, prec, stride=4, draws=8, seed=11)
+    net = proposal.ProposalNet(dev, seed=0)
+    losses = net.train(X, tgt, steps=args.train_steps, batch=65536, lr=3e-3)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    # tensor-core throughput of the network alone on 4M rows
+    R = 1 << 22
+    Xr = torch.randn(R, 16, device=dev)
+    for _ in range(2):
+        net.logits(Xr)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    net.logits(Xr)
+    e1.record(stream)
+    e1.synchronize()
+    t_mlp = e0.elapsed_time(e1) * 1e-3
+    flops = 2.0 * R * (16 * 64 + 64 * 64 * 2 + 64 * 16)
+    seeds = list(range(100, 100 + args.seeds))
+    timed(None, seeds[:2])
+    timed(net, seeds[:2])
+    plain, tp = timed(None, seeds)
+    learned, tl = timed(net, seeds)
+    ep = torch.stack([e for e, _ in plain])
+    el = torch.stack([e for e, _ in learned])
+    live = ep.mean(0) != 0
+    var_p = float(ep.var(0)[live].mean())
+    var_l = float(el.var(0)[live].mean())
+    t_p, t_l = float(np.median(tp)), float(np.median(tl))
+    peaks = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    bf16_peak = json.load(open(peaks)).get("bf16_tflops") if os.path.exists(peaks) else None
+    print(json.dumps({
+        "metric": "time to the plain sampler's estimator variance, learned / plain", "value": (t_l * var_l / var_p) / t_p,
+        "unit": "ratio", "higher_is_better": False, "n_gpus": 1, "dtype": "bf16 network, f32 sampler",
+        "data": "synthetic", "config": {"workload": workload_name("harmonic500k", wl), "seeds": args.seeds,
+                                        "estimate": "weighted mean of the splat albedo (channel 0) per pixel",
+                                        "ess_tau": 0.1},
+        "plain": {"ms_per_call": t_p, "variance": var_p},
+        "learned": {"ms_per_call": t_l, "variance": var_l,
+                    "fallback_pixels_per_call": float(np.mean([n for _, n in learned])),
+                    "train_rows": int(X.shape[0]), "train_steps": args.train_steps, "train_s": t_train,
+                    "final_loss": float(losses[-10:].mean())},
+        "network_tensor_cores": {"rows": R, "ms": t_mlp * 1e3, "tflops": flops / t_mlp / 1e12,
+                                 "peak_bf16_tflops": bf16_peak,
+                                 "frac": (flops / t_mlp / 1e12) / bf16_peak if bf16_peak else None},
+    }), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="harmonic500k", choices=sorted(WORKLOADS) + sorted(MULTIVIEW))
+    ap.add_argument("--workload", default="harmonic500k",
+                    choices=sorted(WORKLOADS) + sorted(MULTIVIEW) + ["proposal"])
+    ap.add_argument("--seeds", type=int, default=8, help="proposal workload: sampling calls per method")
+    ap.add_argument("--train-steps", type=int, default=600, help="proposal workload: Adam steps")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--eager", action="store_true", help="time eager steps instead of a CUDA-graph replay")
     args = ap.parse_args()
+    if args.workload == "proposal":
+        return proposal_main(args)
     if args.workload in MULTIVIEW:
         return multiview_main(args, args.workload, MULTIVIEW[args.workload])
     wl = WORKLOADS[args.workload]
