@@ -72,7 +72,14 @@ typedef struct {
     int32_t tile_x;          /* descent warp tile width in pixels along y:
                                 4, 8, 16 or 32 (0 = 8); results do not depend
                                 on it, only speed (see the autotuner) */
-    int32_t reserved0;
+    int32_t fixed_degree;    /* 0: the reference's adaptive-degree expansions
+                                (P2M per node over its leaves).  4, 6 or 8:
+                                fixed-degree mode (no counterpart in the
+                                reference): every internal node stores a
+                                degree-P expansion built by the M2M shift from
+                                its children's, evaluated where the adaptive
+                                error bound holds at a degree <= P; needs
+                                (N-1)(P+1)^2 floats of coefficient pool */
 } uds_sample_params;
 
 /* ---- transform (transform.cpp:33-86: affineForward/Backward,

@@ -111,7 +111,7 @@ def test_mlp_grad(L, R):
                           err.data_ptr(), torch.cuda.current_stream().cuda_stream) == 0
     torch.cuda.synchronize()
     assert int(err.item()) == 0
-    assert abs(float(lo.item()) - float(loss)) < 1e-3 * abs(float(loss)) + 1e-4
+    assert abs(float(lo.item()) - float(loss.detach())) < 1e-3 * abs(float(loss.detach())) + 1e-4
     Gc = G.cpu()
     o = 0
     for (r, c) in ((64, 16), (64, 64), (64, 64), (16, 64)):

@@ -224,3 +224,35 @@ def test_descent_tile_shapes_agree_and_autotune(smp, tmp_path, monkeypatch):
     assert autotune.lookup(torch.cuda.get_device_name(0), W, H, N, K) == best
     assert torch.equal(smp.sample(*args, seed=3), ref)  # now with the tuned tile
     autotune.reset()
+
+
+@pytest.mark.parametrize("P", [4, 6, 8])
+def test_fixed_degree_m2m(smp, P):
+    """Fixed-degree mode: expansions built by M2M shifts; node masses against
+    the FP64 direct Gauss sums, topology unchanged."""
+    rng = np.random.default_rng(90 + P)
+    W, H, f, N = 64, 56, 60.0, 4000
+    precision = 1e-3
+    pts, nrm, sd = camera_scene(rng, N, W, H, f, sd=(0.01, 0.03))
+    args = (W, H, f, T(pts[None]), T(nrm[None]), T(sd[None]), 8, 0.0, precision)
+    ref = smp.build_tree(*args)
+    tree = smp.build_tree(*args, fixed_degree=P)
+    for k in ("keys", "ids", "left", "right", "parent", "count"):
+        assert torch.equal(tree[k], ref[k]), k
+    n = tree["n_visible"]
+    deg = tree["degree"][: n - 1]
+    assert set(deg.unique().tolist()) <= {-1, P} and (deg == P).any()
+    assert tree["n_coefs"] == (n - 1) * (P + 1) ** 2
+    o = oracle.Tree(W, H, f, pts, tree["h"], oracle.cull_radius(tree["h"], precision), precision)
+    nodes = rng.integers(0, 2 * n - 1, 600).astype(np.int32)
+    q = rng.uniform(0, W, size=(600, 2)).astype(np.float32)
+    got = smp.fgt_eval(tree, T(nodes, torch.int32), T(q)).cpu().numpy()
+    direct = np.array([o.direct_weight(int(v), qq.astype(np.float64)) for v, qq in zip(nodes, q)])
+    err = np.abs(got - direct)
+    assert np.all(err <= 3 * precision + 1e-3 * direct), (P, err.max(), (err / (direct + 1e-9)).max())
+    # the sampler runs on the fixed-degree tree and mostly agrees with the adaptive one
+    a = smp.sample(W, H, f, T(pts[None]), T(nrm[None]), T(np.zeros((1, N, 3))), T(sd[None]), 8, 0.0, precision,
+                   seed=3)
+    b = smp.sample(W, H, f, T(pts[None]), T(nrm[None]), T(np.zeros((1, N, 3))), T(sd[None]), 8, 0.0, precision,
+                   seed=3, fixed_degree=P)
+    assert (a == b).all(-1).float().mean() > 0.9

@@ -505,6 +505,101 @@ __global__ void k_bottomup(const ViewState* vs, float precision, int max_degree,
     }
 }
 
+// ------------------------------------------- 5b fixed-degree M2M pass
+// Fixed-degree mode (no reference counterpart): every internal node stores a
+// degree-P Hermite expansion at offset v * (P+1)^2, obtained from its
+// children's by the M2M shift instead of summing over its leaves:
+//   M_ab(c) = sum_{a' <= a, b' <= b} M_a'b'(c_child) t_{a-a'}(dx) t_{b-b'}(dy),
+// t_k(d) = d^k / k!, (dx, dy) = (c_child - c) / sqrt(2 h^2); a leaf child is
+// the single moment M_00 = 1 at its own position.  Exact for the truncated
+// moments (the moments of the union are polynomial in the shift), so the
+// expansions equal the per-leaf sums up to rounding at O(P^3) per node.  The
+// node is evaluated through its expansion (degree P) when the adaptive error
+// bound holds at some degree <= P (k_bottomup run with max_degree = P), else
+// walked (degree -1); the coefficients exist either way for the parent's
+// shift.  Same second-arrival fan-in as k_bottomup.
+__global__ void k_fixed_assign(ViewState* vs, float4* cen, int P) {
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    int n = vs->n;
+    if (v == 0) vs->coef_used = (unsigned)((n > 1 ? n - 1 : 0) * (P + 1) * (P + 1));
+    if (v >= n - 1) return;
+    float4 c = cen[v];
+    c.w = make_meta(v * (P + 1) * (P + 1), meta_degree(c.w) >= 0 ? P : -1);
+    cen[v] = c;
+}
+
+template <int P>
+__global__ void k_m2m(const ViewState* vs, const int4* __restrict__ lnk, const int* __restrict__ par,
+                      const float4* __restrict__ cen, float* coef, unsigned* fanin) {
+    constexpr int P1 = P + 1, P2 = P1 * P1;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int n = vs->n;
+    if (i >= n || n < 2) return;
+    float sq = vs->sq;
+    int v = n - 1 + i;
+    while (true) {
+        int p = par[v];
+        if (p < 0) break;
+        __threadfence();
+        if (atomicAdd(&fanin[p], 1u) == 0) return;
+        __threadfence();
+        int4 L = lnk[p];
+        float4 cp = cen[p];
+        float acc[P1][P1];
+#pragma unroll
+        for (int a = 0; a < P1; ++a)
+#pragma unroll
+            for (int b = 0; b < P1; ++b) acc[a][b] = 0.0f;
+#pragma unroll
+        for (int side = 0; side < 2; ++side) {
+            int c = side ? L.y : L.x;
+            float4 cc = cen[c];
+            float dx = (cc.x - cp.x) / sq, dy = (cc.y - cp.y) / sq;
+            float tx[P1], ty[P1];
+            tx[0] = 1.0f;
+            ty[0] = 1.0f;
+#pragma unroll
+            for (int k = 1; k < P1; ++k) {
+                tx[k] = tx[k - 1] * dx / (float)k;
+                ty[k] = ty[k - 1] * dy / (float)k;
+            }
+            if (c >= n - 1) {
+#pragma unroll
+                for (int a = 0; a < P1; ++a)
+#pragma unroll
+                    for (int b = 0; b < P1; ++b) acc[a][b] = fmaf(tx[a], ty[b], acc[a][b]);
+            } else {
+                const float* C = coef + (size_t)c * P2;
+                float D[P1][P1];  // shift along y first
+#pragma unroll
+                for (int a = 0; a < P1; ++a)
+#pragma unroll
+                    for (int b = 0; b < P1; ++b) {
+                        float sum = 0.0f;
+#pragma unroll
+                        for (int bb = 0; bb <= b; ++bb) sum = fmaf(__ldcg(C + a * P1 + bb), ty[b - bb], sum);
+                        D[a][b] = sum;
+                    }
+#pragma unroll
+                for (int a = 0; a < P1; ++a)
+#pragma unroll
+                    for (int b = 0; b < P1; ++b) {
+                        float sum = acc[a][b];
+#pragma unroll
+                        for (int aa = 0; aa <= a; ++aa) sum = fmaf(D[aa][b], tx[a - aa], sum);
+                        acc[a][b] = sum;
+                    }
+            }
+        }
+        float* out = coef + (size_t)p * P2;
+#pragma unroll
+        for (int a = 0; a < P1; ++a)
+#pragma unroll
+            for (int b = 0; b < P1; ++b) __stcg(out + a * P1 + b, acc[a][b]);
+        v = p;
+    }
+}
+
 // ------------------------------------------------ 6 coefficient offsets
 __global__ void k_node_sizes(const ViewState* vs, const float4* __restrict__ cen, uint32_t* __restrict__ sizes) {
     int v = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1402,6 +1497,20 @@ static int build_view(const uds_sample_params* p, const Ws& w, int view, const f
     k_leaves<<<nbN, 128, 0, s>>>(N, W, H, f, vp, w.vs, p->precision, vi, w.leaf_xy, w.leaf_id, w.lnk, w.par,
                                  w.box, w.cen);
     k_karras<<<nbN, 128, 0, s>>>(w.vs, ki, w.lnk, w.par);
+    if (p->fixed_degree > 0) {
+        int P = p->fixed_degree;
+        k_bottomup<<<nbN, 128, 0, s>>>(w.vs, p->precision, P, w.lnk, w.par, w.box, w.cen, w.fanin);
+        k_fixed_assign<<<nbN, 128, 0, s>>>(w.vs, w.cen, P);
+        e = cudaMemsetAsync(w.fanin, 0, 4 * (size_t)N, s);
+        if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
+        switch (P) {
+            case 4: k_m2m<4><<<nbN, 128, 0, s>>>(w.vs, w.lnk, w.par, w.cen, w.coef, w.fanin); break;
+            case 6: k_m2m<6><<<nbN, 128, 0, s>>>(w.vs, w.lnk, w.par, w.cen, w.coef, w.fanin); break;
+            default: k_m2m<8><<<nbN, 128, 0, s>>>(w.vs, w.lnk, w.par, w.cen, w.coef, w.fanin); break;
+        }
+        k_finish_view<<<1, 1, 0, s>>>(w.vs, w.stats + view);
+        return launch_status(6);
+    }
     k_bottomup<<<nbN, 128, 0, s>>>(w.vs, p->precision, p->max_degree, w.lnk, w.par, w.box, w.cen, w.fanin);
     k_node_sizes<<<nbN, 128, 0, s>>>(w.vs, w.cen, w.sizes);
     if ((st = launch_status(4))) return st;
@@ -1454,6 +1563,12 @@ static int check_params(const uds_sample_params* p) {
     if ((size_t)p->N * 2 >= (1u << 31)) return UDS_ERR_ARGUMENT;
     if (p->tile_x != 0 && p->tile_x != 4 && p->tile_x != 8 && p->tile_x != 16 && p->tile_x != 32)
         return UDS_ERR_ARGUMENT;
+    if (p->fixed_degree != 0) {
+        if (p->fixed_degree != 4 && p->fixed_degree != 6 && p->fixed_degree != 8) return UDS_ERR_ARGUMENT;
+        int64_t need = (int64_t)(p->N > 1 ? p->N - 1 : 0) * (p->fixed_degree + 1) * (p->fixed_degree + 1);
+        int64_t cap = p->coef_pool > 0 ? p->coef_pool : default_pool(p->N);
+        if (need > cap) return UDS_ERR_ARGUMENT;  // one expansion per internal node must fit the pool
+    }
     int64_t pool = p->coef_pool > 0 ? p->coef_pool : default_pool(p->N);
     if (pool >= (1ll << 26)) return UDS_ERR_ARGUMENT;  // offsets are packed in 26 bits
     return UDS_OK;

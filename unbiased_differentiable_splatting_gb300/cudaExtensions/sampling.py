@@ -14,6 +14,9 @@ end so existing calls keep working:
   torch's CPU generator.
 * ``h``: (B,) float32 CUDA tensor of bandwidths that replace the computed ones
   (entries <= 0 keep the computed value).
+* ``fixed_degree``: 0 (the reference's adaptive expansions) or 4, 6, 8: every
+  internal node gets a degree-P expansion built by the M2M shift from its
+  children (no reference counterpart; not bit-identical to the oracle).
 * ``tile_x``: width of the descent's 32-pixel warp tiles (4, 8, 16, 32);
   default: the autotuner's cached choice for this shape (see ``autotune``),
   else 8.  The indices do not depend on it.
@@ -42,14 +45,14 @@ def num_rounds(K: int) -> int:
 
 
 def params(width, height, focallength, points, stdDevs, numSamples, smoothing, precision, seed=0,
-           max_degree=MAX_DEGREE, coef_pool=0, tile_x=0) -> SampleParams:
+           max_degree=MAX_DEGREE, coef_pool=0, tile_x=0, fixed_degree=0) -> SampleParams:
     """``seed``: an int, or a one-element int64 CUDA tensor whose value the
     kernels read when they run (a captured CUDA graph then draws new numbers
     after the tensor is updated)."""
     prm = SampleParams(B=points.shape[0], N=points.shape[1], W=int(width), H=int(height), K=int(numSamples),
                        focal=float(focallength), smoothing=float(smoothing), precision=float(precision),
                        max_degree=int(max_degree), std_batch=stdDevs.shape[0], coef_pool=int(coef_pool or 0),
-                       seed=0, seed_dev=None, tile_x=int(tile_x or 0), reserved0=0)
+                       seed=0, seed_dev=None, tile_x=int(tile_x or 0), fixed_degree=int(fixed_degree or 0))
     if isinstance(seed, torch.Tensor):
         if seed.dtype != torch.int64 or seed.numel() != 1 or seed.device != points.device:
             raise ValueError("a seed tensor must be one int64 element on the points' device")
@@ -96,7 +99,7 @@ _device_names = {}
 
 def sample(width: int, height: int, focallength: float, points, normals, colors, stdDevs, numSamples: int,
            smoothing: float, precision: float, uniforms=None, seed=None, h=None, return_stats=False,
-           max_degree=MAX_DEGREE, coef_pool=0, tile_x=None):
+           max_degree=MAX_DEGREE, coef_pool=0, tile_x=None, fixed_degree=0):
     _check(points, normals, stdDevs)
     dev = points.device
     B = points.shape[0]
@@ -104,7 +107,7 @@ def sample(width: int, height: int, focallength: float, points, normals, colors,
     if seed is None:
         seed = int(torch.randint(0, 2 ** 62, (1,)).item())
     prm = params(width, height, focallength, points, stdDevs, K, smoothing, precision, seed, max_degree, coef_pool,
-                 _tile(points, width, height, K, tile_x))
+                 _tile(points, width, height, K, tile_x), fixed_degree)
     if uniforms is not None:
         need(uniforms, "uniforms", device=dev)
         R = num_rounds(K)
@@ -163,14 +166,14 @@ def view_stats(stats: torch.Tensor) -> dict:
 
 
 def build_tree(width, height, focallength, points, normals, stdDevs, numSamples, smoothing, precision, view=0,
-               h=None, max_degree=MAX_DEGREE, coef_pool=0):
+               h=None, max_degree=MAX_DEGREE, coef_pool=0, fixed_degree=0):
     """Build one view's tree and return its arrays (test / debug helper of
     uds_tree_build).  Keeps the workspace for fgt_eval."""
     _check(points, normals, stdDevs)
     dev = points.device
     N = points.shape[1]
     prm = params(width, height, focallength, points, stdDevs, numSamples, smoothing, precision, 0, max_degree,
-                 coef_pool)
+                 coef_pool, 0, fixed_degree)
     L = load()
     ws = Workspace.get(dev, workspace_bytes(prm), "tree")
     M = max(2 * N - 1, 1)
