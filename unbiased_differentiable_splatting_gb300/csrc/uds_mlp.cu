@@ -125,6 +125,15 @@ __device__ __forceinline__ void put_bf16(unsigned char* base, uint32_t off, floa
     *reinterpret_cast<__nv_bfloat16*>(base + off) = __float2bfloat16_rn(v);
 }
 
+// Row r, elements k0 .. k0+7 (k0 a multiple of 8) of a K-major operand are one
+// 16-byte core-matrix row: store them with one vector store.
+__device__ __forceinline__ void put8_bf16(unsigned char* base, int r, int k0, int K, const float* v) {
+    __nv_bfloat162 h[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) h[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+    *reinterpret_cast<uint4*>(base + tc::kmajor_offset(r, k0, K)) = *reinterpret_cast<uint4*>(h);
+}
+
 // Stage an fp32 [R x K] row-major matrix as bf16 K-major operand.
 __device__ __forceinline__ void stage_matrix(unsigned char* dst, const float* src, int R, int K) {
     for (int i = threadIdx.x; i < R * K; i += blockDim.x) put_bf16(dst, tc::kmajor_offset(i / K, i % K, K), src[i]);
@@ -186,9 +195,17 @@ __global__ void __launch_bounds__(128) k_mlp_forward(int R, const int* __restric
     for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
         int row = t * kTile + tid;
         // features -> bf16 A operand (rows past R are zero)
+        {
+            float xv[kIn];
+            const float4* xr = reinterpret_cast<const float4*>(X + (size_t)row * kIn);
 #pragma unroll
-        for (int k = 0; k < kIn; ++k)
-            put_bf16(S.x, tc::kmajor_offset(tid, k, kIn), row < R ? X[(size_t)row * kIn + k] : 0.0f);
+            for (int q = 0; q < kIn / 4; ++q) {
+                float4 f4 = row < R ? xr[q] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                xv[4 * q] = f4.x; xv[4 * q + 1] = f4.y; xv[4 * q + 2] = f4.z; xv[4 * q + 3] = f4.w;
+            }
+            put8_bf16(S.x, tid, 0, kIn, xv);
+            put8_bf16(S.x, tid, 8, kIn, xv + 8);
+        }
         tc::fence_async_smem();
         __syncthreads();
         const unsigned char* a = S.x;
@@ -203,8 +220,9 @@ __global__ void __launch_bounds__(128) k_mlp_forward(int R, const int* __restric
                 float v[16];
                 tc::tmem_ld16(lane_base + (uint32_t)c0, v);
 #pragma unroll
-                for (int c = 0; c < 16; ++c)
-                    put_bf16(S.h, tc::kmajor_offset(tid, c0 + c, kHid), fmaxf(v[c] + S.bias[l * kHid + c0 + c], 0.0f));
+                for (int c = 0; c < 16; ++c) v[c] = fmaxf(v[c] + S.bias[l * kHid + c0 + c], 0.0f);
+                put8_bf16(S.h, tid, c0, kHid, v);
+                put8_bf16(S.h, tid, c0 + 8, kHid, v + 8);
             }
             tc::fence_before_sync();
             tc::fence_async_smem();
@@ -335,9 +353,17 @@ __global__ void __launch_bounds__(128) k_mlp_grad(int R, const float* __restrict
     for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
         int row = t * kTile + tid;
         bool valid = row < R;
+        {
+            float xv[kIn];
+            const float4* xr = reinterpret_cast<const float4*>(X + (size_t)row * kIn);
 #pragma unroll
-        for (int k = 0; k < kIn; ++k)
-            put_bf16(S.x, tc::kmajor_offset(tid, k, kIn), valid ? X[(size_t)row * kIn + k] : 0.0f);
+            for (int q = 0; q < kIn / 4; ++q) {
+                float4 f4 = valid ? xr[q] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                xv[4 * q] = f4.x; xv[4 * q + 1] = f4.y; xv[4 * q + 2] = f4.z; xv[4 * q + 3] = f4.w;
+            }
+            put8_bf16(S.x, tid, 0, kIn, xv);
+            put8_bf16(S.x, tid, 8, kIn, xv + 8);
+        }
         tc::fence_async_smem();
         __syncthreads();
         // ---- forward
@@ -351,9 +377,9 @@ __global__ void __launch_bounds__(128) k_mlp_grad(int R, const float* __restrict
                 float v[16];
                 tc::tmem_ld16(lane_base + (uint32_t)c0, v);
 #pragma unroll
-                for (int c = 0; c < 16; ++c)
-                    put_bf16(S.h[l], tc::kmajor_offset(tid, c0 + c, kHid),
-                             fmaxf(v[c] + S.bias[l * kHid + c0 + c], 0.0f));
+                for (int c = 0; c < 16; ++c) v[c] = fmaxf(v[c] + S.bias[l * kHid + c0 + c], 0.0f);
+                put8_bf16(S.h[l], tid, c0, kHid, v);
+                put8_bf16(S.h[l], tid, c0 + 8, kHid, v + 8);
             }
             tc::fence_before_sync();
             tc::fence_async_smem();
