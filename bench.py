@@ -175,7 +175,7 @@ def cpu_sample(wl, scene, target_s=12.0):
 
 def profiled_traffic(kernel="k_sample"):
     """DRAM bytes per launch of `kernel` from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "k_sample_k_p2m_harmonic500k_1024.md")
+    path = os.path.join(ROOT, "profiles", "k_sample_harmonic500k_1024.md")
     try:
         for line in open(path):
             if line.startswith(f"traffic_bytes_per_launch {kernel}:"):
@@ -679,7 +679,7 @@ def main():
             "eager_ms_per_step": t_eager,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": profiled_traffic() if args.workload == "harmonic500k" else None,
-                         "traffic_source": "ncu capture, profiles/k_sample_k_p2m_harmonic500k_1024.md",
+                         "traffic_source": "ncu capture, profiles/k_sample_harmonic500k_1024.md",
                          "kernel": "k_sample (per-pixel descent)",
                          "kernel_ms": t_desc * 1e3, "bytes_alg": int(bytes_alg), "peak_source": peak_src},
             "cpu_baseline": cpu,
