@@ -997,10 +997,15 @@ __global__ void __launch_bounds__(128, 3) k_sample(Tree T, const ViewState* vs, 
     float keys[KM];
 #pragma unroll UK
     for (int k = 0; k < KM; ++k) { ids[k] = -1; keys[k] = __int_as_float(0x7f800000); }
-    int tn[R][kTrace];
+    // each round's path is kept as its choice bits (bit m: right child taken
+    // at depth m) and its length, in registers: two rounds meet the same node
+    // at depth m iff their first m choices agree (node ids are unique)
+    unsigned long long pb[R];
     float tc[R][kTrace];
     float tp[kTrace];
     int tl[R];
+#pragma unroll
+    for (int rr = 0; rr < R; ++rr) { pb[rr] = 0ull; tl[rr] = 0; }
     // child masses of the node met at each depth by the latest round; slots
     // [0, cvn) are valid (depths are reached in order, so no clearing needed)
     int cv[kTrace];
@@ -1031,7 +1036,7 @@ __global__ void __launch_bounds__(128, 3) k_sample(Tree T, const ViewState* vs, 
         }
         int v = 0, d = 0;
         int e = (mc.ok && mc.m > 0) ? 0 : -1;  // cache entry of v
-        tn[r][0] = 0;
+        unsigned long long cur = 0ull;         // this round's choice bits so far
         tp[0] = 1.0f;
         int4 L = T.lnk[0];
         bool going = act && L.w > K;
@@ -1070,20 +1075,28 @@ __global__ void __launch_bounds__(128, 3) k_sample(Tree T, const ViewState* vs, 
                 pend &= ~grp;
             }
             if (going) {
-                if (!(d < cvn && cv[d] == v)) {
-                    cv[d] = v;
-                    cw0[d] = w0;
-                    cw1[d] = w1;
-                    if (d >= cvn) cvn = d + 1;
-                }
+                // (re)write unconditionally: a hit stores the same masses, and
+                // a store does not wait on the per-thread memory like a load
+                cv[d] = v;
+                cw0[d] = w0;
+                cw1[d] = w1;
+                if (d >= cvn) cvn = d + 1;
                 float sum = fadd(fadd(0.0f, w0), w1);
                 w0 = fdiv(w0, sum);
                 w1 = fdiv(w1, sum);
+                // capacities of a and b: from the latest earlier round whose
+                // path passed through v (same first d choices) into that child
                 float c0 = 1.0f, c1 = 1.0f;
-                for (int rr = r - 1; rr >= 0; --rr)
-                    if (d + 1 < tl[rr] && tn[rr][d + 1] == a) { c0 = tc[rr][d + 1]; break; }
-                for (int rr = r - 1; rr >= 0; --rr)
-                    if (d + 1 < tl[rr] && tn[rr][d + 1] == b) { c1 = tc[rr][d + 1]; break; }
+                bool f0 = false, f1 = false;
+                unsigned long long pre = (1ull << d) - 1ull;
+#pragma unroll
+                for (int rr = R - 1; rr >= 0; --rr) {
+                    if (rr < r && d + 1 < tl[rr] && ((pb[rr] ^ cur) & pre) == 0ull) {
+                        bool right = (pb[rr] >> d) & 1ull;
+                        if (!right && !f0) { c0 = tc[rr][d + 1]; f0 = true; }
+                        if (right && !f1) { c1 = tc[rr][d + 1]; f1 = true; }
+                    }
+                }
                 float s0 = fmul(w0, c0), s1 = fmul(w1, c1);
                 ++d;
                 if (d >= kTrace) {
@@ -1091,20 +1104,25 @@ __global__ void __launch_bounds__(128, 3) k_sample(Tree T, const ViewState* vs, 
                     going = false;
                     act = false;
                 } else {
-                    if (s0 < s1) { tn[r][d] = b; tp[d] = w1; v = b; e = eb; }
-                    else { tn[r][d] = a; tp[d] = w0; v = a; e = ea; }
+                    if (s0 < s1) { cur |= 1ull << (d - 1); tp[d] = w1; v = b; e = eb; }
+                    else { tp[d] = w0; v = a; e = ea; }
                     L = T.lnk[v];
                     going = L.w > K;
                 }
             }
         }
         if (!act) continue;
-        tl[r] = d + 1;
+#pragma unroll
+        for (int rr = 0; rr < R; ++rr)
+            if (rr == r) { pb[rr] = cur; tl[rr] = d + 1; }
         float prob = 1.0f;
         for (int m = d; m >= 0; --m) {
             float cap = 1.0f;
-            for (int rr = r - 1; rr >= 0; --rr)
-                if (m < tl[rr] && tn[rr][m] == tn[r][m]) { cap = tc[rr][m]; break; }
+            bool found = false;
+            unsigned long long pre = (1ull << m) - 1ull;
+#pragma unroll
+            for (int rr = R - 1; rr >= 0; --rr)
+                if (rr < r && !found && m < tl[rr] && ((pb[rr] ^ cur) & pre) == 0ull) { cap = tc[rr][m]; found = true; }
             tc[r][m] = fmaxf(0.0f, fsub(cap, prob));
             prob = fmul(prob, tp[m]);
         }
