@@ -160,6 +160,19 @@ int uds_sample_descent(const uds_sample_params* prm, int view, const float* unif
 int uds_fgt_eval(const uds_sample_params* prm, int m, const int32_t* nodes, const float* query_xy,
                  float* out, const void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---- pixelgather.scatter / gather (pixelGather.cpp:10-24,
+ *      pixelGatherCuda.cu:7-152).  scatter: out (B,W,H,K,C) = values (B,N,C)
+ *      at each sample's splat, 0 for index -1.  gather: out (B,N,C) = sum of
+ *      values (B,W,H,K,C) over the samples of each splat; deterministic = 0
+ *      adds with atomics (unordered, as the reference), deterministic = 1 sums
+ *      each splat's samples in sample order (bit-reproducible; workspace
+ *      uds_pixel_gather_workspace_size bytes, unused otherwise). ---- */
+int uds_pixel_scatter(int B, int W, int H, int K, const int32_t* indices, int N, int C, const float* values,
+                      float* out, void* stream);
+size_t uds_pixel_gather_workspace_size(int B, int W, int H, int K, int N);
+int uds_pixel_gather(int B, int W, int H, int K, const int32_t* indices, int N, int C, const float* values,
+                     float* out, int deterministic, void* workspace, size_t workspace_bytes, void* stream);
+
 /* ---- proposal network (no counterpart in the reference).  Tensor-core
  *      kernels (tcgen05, accumulators in tensor memory). ---- */
 /* Layout check of the tensor-core path (debug): C (128 x N, fp32) =

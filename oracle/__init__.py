@@ -215,6 +215,25 @@ def interp_backward(gin, idx, w, attr):
     return gw, ga
 
 
+# --------------------------------------------------------------- pixelgather
+def pixel_scatter(idx, values):
+    idx, values = _i(idx), _f(values)
+    B, W, H, K = idx.shape
+    N, Cn = values.shape[1], values.shape[2]
+    out = np.zeros((B, W, H, K, Cn), np.float32)
+    lib().orc_pixel_scatter(C(B), C(W), C(H), C(K), P(idx), C(N), C(Cn), P(values), P(out))
+    return out
+
+
+def pixel_gather(idx, values, N):
+    idx, values = _i(idx), _f(values)
+    B, W, H, K = idx.shape
+    Cn = values.shape[4]
+    out = np.zeros((B, N, Cn), np.float32)
+    lib().orc_pixel_gather(C(B), C(W), C(H), C(K), P(idx), C(N), C(Cn), P(values), P(out))
+    return out
+
+
 # ------------------------------------------------------------------ shading
 def shade_forward(dirs, I, nrm, dif):
     dirs, I, nrm, dif = _f(dirs), _f(I), _f(nrm), _f(dif)

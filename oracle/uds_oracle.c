@@ -1384,3 +1384,34 @@ int orc_sample_view(int W, int H, float f, int N, const float* pts, const float*
     orc_tree_free(t);
     return st;
 }
+
+/* scatterKernel (pixelGatherCuda.cu:7-36): each sample takes its splat's
+ * channels; samples with index -1 stay 0 (the reference zero-fills the output
+ * and skips them). */
+void orc_pixel_scatter(int B, int W, int H, int K, const int* idx, int N, int C, const float* values,
+                       float* out) {
+    size_t per_view = (size_t)W * H * K;
+    for (int b = 0; b < B; ++b)
+        for (size_t t = 0; t < per_view; ++t) {
+            size_t s = t + per_view * (size_t)b;
+            int id = idx[s];
+            for (int c = 0; c < C; ++c)
+                out[s * (size_t)C + c] = (id >= 0 && id < N) ? values[((size_t)id + (size_t)N * b) * C + c] : 0.0f;
+        }
+}
+
+/* gatherKernel (pixelGatherCuda.cu:78-110): each sample's channels added to
+ * its splat; the reference adds with atomics in no fixed order, here in
+ * sample order (the order the deterministic GPU mode reproduces). */
+void orc_pixel_gather(int B, int W, int H, int K, const int* idx, int N, int C, const float* values,
+                      float* out) {
+    size_t per_view = (size_t)W * H * K;
+    for (size_t i = 0; i < (size_t)B * N * C; ++i) out[i] = 0.0f;
+    for (int b = 0; b < B; ++b)
+        for (size_t t = 0; t < per_view; ++t) {
+            size_t s = t + per_view * (size_t)b;
+            int id = idx[s];
+            if (id < 0 || id >= N) continue;
+            for (int c = 0; c < C; ++c) out[((size_t)id + (size_t)N * b) * C + c] += values[s * (size_t)C + c];
+        }
+}

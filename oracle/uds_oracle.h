@@ -74,6 +74,13 @@ void orc_interp_backward(int B, int W, int H, int K, const float* gin, const int
                          const float* w, int aB, int N, int C, const float* attr, float* gw,
                          float* ga);
 
+/* pixelgather (pixelGatherCuda.cu:7-152): scatter (B,N,C) -> (B,W,H,K,C);
+ * gather (B,W,H,K,C) -> (B,N,C), each splat's samples summed in sample order */
+void orc_pixel_scatter(int B, int W, int H, int K, const int* idx, int N, int C, const float* values,
+                       float* out);
+void orc_pixel_gather(int B, int W, int H, int K, const int* idx, int N, int C, const float* values,
+                      float* out);
+
 /* shading.cpp:51-199, shadingCuda.cu, diffuseShading*.cuh */
 void orc_shade_forward(int B, int P, int L, const float* dirs, const float* I, int IB,
                        const float* nrm, const float* dif, float* out);

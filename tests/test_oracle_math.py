@@ -253,3 +253,20 @@ def test_stochastic_mode_chi_square():
         stat = np.sum((Ob[keep] - Eb[keep]) ** 2 / Eb[keep])
         pvals.append(chi2.sf(stat, max(int(keep.sum()) - 1, 1)))
     assert min(pvals) > 1e-3 / len(pvals), pvals
+
+
+def test_pixel_scatter_gather_oracle():
+    """scatter copies each sample's splat row; gather is its adjoint
+    (<scatter(v), g> = <v, gather(g)>), index -1 contributes nothing."""
+    rng = np.random.default_rng(9)
+    B, W, H, K, N, Cn = 2, 5, 4, 3, 7, 3
+    idx = rng.integers(-1, N, size=(B, W, H, K)).astype(np.int32)
+    v = rng.normal(size=(B, N, Cn)).astype(np.float32)
+    g = rng.normal(size=(B, W, H, K, Cn)).astype(np.float32)
+    s = oracle.pixel_scatter(idx, v)
+    for b in range(B):
+        m = idx[b] >= 0
+        np.testing.assert_array_equal(s[b][m], v[b][idx[b][m]])
+        assert np.all(s[b][~m] == 0)
+    gt = oracle.pixel_gather(idx, g, N)
+    assert abs(float((s * g).sum()) - float((v * gt).sum())) < 1e-4

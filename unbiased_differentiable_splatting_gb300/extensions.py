@@ -13,7 +13,7 @@ from __future__ import annotations
 
 import torch as th
 
-from .cudaExtensions import filtering, interpolation, sampling, shading, splatting, transform
+from .cudaExtensions import filtering, interpolation, pixelgather, sampling, shading, splatting, transform
 
 
 # ------------------------------------------------------------------ utils
@@ -187,3 +187,21 @@ class SphericalHarmonicShading(th.autograd.Function):
 __all__ = ["FmmSampling", "AffineTransform", "LinearTransform", "EWASplatting", "DepthFiltering",
            "LinearInterpolation", "DiffuseShading", "SphericalHarmonicShading", "world2Camera", "transformForward",
            "conditionalNormalization", "normalize", "dot"]
+
+
+# ------------------------------------------------------------ pixel gather
+class PixelScatterGather(th.autograd.Function):
+    """extensions/__init__.py:407-437: per-sample splat attributes
+    (B,W,H,K,C) from (B,N,C); the backward sums each sample's gradient back
+    onto its splat."""
+
+    @staticmethod
+    def forward(ctx, indices, values):
+        ctx.save_for_backward(indices)
+        ctx.numSources = values.shape[1]
+        return pixelgather.scatter(indices, values.contiguous())
+
+    @staticmethod
+    def backward(ctx, grad_output):
+        (indices,) = ctx.saved_tensors
+        return None, pixelgather.gather(indices, grad_output.contiguous(), ctx.numSources)
