@@ -173,6 +173,19 @@ size_t uds_pixel_gather_workspace_size(int B, int W, int H, int K, int N);
 int uds_pixel_gather(int B, int W, int H, int K, const int32_t* indices, int N, int C, const float* values,
                      float* out, int deterministic, void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---- nearestsamples.nearest (nearestSamples.cpp:31-75,
+ *      nearestSamplesCuda.cu:355-564): for every splat s, the num_nearest
+ *      (<= 32) nearest splats among the other samples of the pixels whose
+ *      surface sample (largest weight, first on ties) is s; distances between
+ *      points (1,N,3); nearest (1,N,num_nearest) int32 ordered by (distance,
+ *      index), -1 padded (the reference's lock-order-dependent merge and its
+ *      infinite-distance padding are replaced by this order-free
+ *      definition).  indices, weights (B,W,H,K). ---- */
+size_t uds_nearest_workspace_size(int B, int W, int H, int K, int N);
+int uds_nearest_samples(int B, int W, int H, int K, const int32_t* indices, const float* weights, int N,
+                        const float* points, int num_nearest, int32_t* nearest, void* workspace,
+                        size_t workspace_bytes, void* stream);
+
 /* ---- proposal network (no counterpart in the reference).  Tensor-core
  *      kernels (tcgen05, accumulators in tensor memory). ---- */
 /* Layout check of the tensor-core path (debug): C (128 x N, fp32) =

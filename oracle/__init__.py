@@ -234,6 +234,15 @@ def pixel_gather(idx, values, N):
     return out
 
 
+def nearest_samples(idx, w, pts, M):
+    idx, w, pts = _i(idx), _f(w), _f(pts).reshape(-1, 3)
+    B, W, H, K = idx.shape
+    N = pts.shape[0]
+    out = np.full((N, M), -1, np.int32)
+    lib().orc_nearest_samples(C(B), C(W), C(H), C(K), P(idx), P(w), C(N), P(pts), C(M), P(out))
+    return out
+
+
 # ------------------------------------------------------------------ shading
 def shade_forward(dirs, I, nrm, dif):
     dirs, I, nrm, dif = _f(dirs), _f(I), _f(nrm), _f(dif)

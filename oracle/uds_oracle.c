@@ -1415,3 +1415,53 @@ void orc_pixel_gather(int B, int W, int H, int K, const int* idx, int N, int C, 
             for (int c = 0; c < C; ++c) out[((size_t)id + (size_t)N * b) * C + c] += values[s * (size_t)C + c];
         }
 }
+
+/* nearestsamples.nearest (nearestSamplesCuda.cu:355-454): the surface
+ * sample of a pixel is its largest-weight sample (first on ties,
+ * :375-386); the pixel's other valid samples are candidates for it.  The
+ * reference merges them under a lock (order dependent); this restatement
+ * keeps, per splat, the M distinct candidates of smallest distance, ties by
+ * index. */
+static float orc_pdist(const float* pts, int a, int b) {
+    float dx = pts[3 * a] - pts[3 * b], dy = pts[3 * a + 1] - pts[3 * b + 1], dz = pts[3 * a + 2] - pts[3 * b + 2];
+    return sqrtf(dx * dx + dy * dy + dz * dz);
+}
+
+void orc_nearest_samples(int B, int W, int H, int K, const int* idx, const float* w, int N, const float* pts, int M,
+                         int* out) {
+    float* bd = (float*)malloc(sizeof(float) * (size_t)N * M);
+    for (size_t i = 0; i < (size_t)N * M; ++i) out[i] = -1;
+    int* cnt = (int*)calloc((size_t)N, sizeof(int));
+    size_t P = (size_t)B * W * H;
+    for (size_t pix = 0; pix < P; ++pix) {
+        const int* id = idx + pix * K;
+        const float* wt = w + pix * K;
+        int s = id[0];
+        float sw = wt[0];
+        for (int k = 1; k < K; ++k)
+            if (wt[k] > sw) { sw = wt[k]; s = id[k]; }
+        if (s < 0 || s >= N) continue;
+        for (int k = 0; k < K; ++k) {
+            int c = id[k];
+            if (c < 0 || c >= N || c == s) continue;
+            int* li = out + (size_t)s * M;
+            float* ld = bd + (size_t)s * M;
+            int m = cnt[s], dup = 0;
+            for (int q = 0; q < m; ++q) dup |= li[q] == c;
+            if (dup) continue;
+            float d = orc_pdist(pts, s, c);
+            if (m == M && !(d < ld[M - 1] || (d == ld[M - 1] && c < li[M - 1]))) continue;
+            int q = m < M ? m++ : M - 1;
+            while (q > 0 && (d < ld[q - 1] || (d == ld[q - 1] && c < li[q - 1]))) {
+                ld[q] = ld[q - 1];
+                li[q] = li[q - 1];
+                --q;
+            }
+            ld[q] = d;
+            li[q] = c;
+            cnt[s] = m;
+        }
+    }
+    free(cnt);
+    free(bd);
+}

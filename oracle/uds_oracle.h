@@ -81,6 +81,11 @@ void orc_pixel_scatter(int B, int W, int H, int K, const int* idx, int N, int C,
 void orc_pixel_gather(int B, int W, int H, int K, const int* idx, int N, int C, const float* values,
                       float* out);
 
+/* nearestsamples.nearest: per splat, the M nearest distinct candidates in
+ * (distance, index) order, -1 padded; out (N x M) */
+void orc_nearest_samples(int B, int W, int H, int K, const int* idx, const float* w, int N, const float* pts, int M,
+                         int* out);
+
 /* shading.cpp:51-199, shadingCuda.cu, diffuseShading*.cuh */
 void orc_shade_forward(int B, int P, int L, const float* dirs, const float* I, int IB,
                        const float* nrm, const float* dif, float* out);

@@ -70,6 +70,9 @@ _SIGS = {
     "uds_pixel_gather_workspace_size": (c_size_t, [c_int, c_int, c_int, c_int, c_int]),
     "uds_pixel_gather": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_int, c_int, c_void_p, c_void_p, c_int,
                                  c_void_p, c_size_t, c_void_p]),
+    "uds_nearest_workspace_size": (c_size_t, [c_int, c_int, c_int, c_int, c_int]),
+    "uds_nearest_samples": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_int,
+                                    c_void_p, c_void_p, c_size_t, c_void_p]),
     "uds_splat_workspace_size": (c_size_t, [c_int, c_int]),
     "uds_splat_forward": (c_int, [c_int, c_int, c_int, c_int, c_float, c_void_p, c_void_p, c_void_p, c_int,
                                   c_int, c_void_p, c_float, c_void_p, c_void_p, c_size_t, c_void_p]),

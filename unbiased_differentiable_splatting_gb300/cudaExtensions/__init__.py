@@ -5,6 +5,6 @@ thin host wrapper over the C ABI of libuds.so running on the current CUDA
 stream.  Inputs are validated (contiguous float32 / int32 CUDA tensors on one
 device) and a bad input raises instead of asserting.
 """
-from . import filtering, interpolation, pixelgather, sampling, shading, splatting, transform  # noqa: F401
+from . import filtering, interpolation, nearestsamples, pixelgather, sampling, shading, splatting, transform  # noqa: F401,E501
 
-__all__ = ["transform", "sampling", "splatting", "filtering", "interpolation", "shading", "pixelgather"]
+__all__ = ["transform", "sampling", "splatting", "filtering", "interpolation", "shading", "pixelgather", "nearestsamples"]
