@@ -186,6 +186,23 @@ int uds_nearest_samples(int B, int W, int H, int K, const int32_t* indices, cons
                         const float* points, int num_nearest, int32_t* nearest, void* workspace,
                         size_t workspace_bytes, void* stream);
 
+/* ---- training-step tail (optimization_geometry.py:190-219), fused.
+ *      uds_image_loss: kind 0 = L1, 1 = L2 (losses.py:5-31); *loss =
+ *      scale * sum over the n elements, grad = d(*loss)/dx (scale = 1 for
+ *      reduction 'sum', 1/n for 'mean').
+ *      uds_adam_splats: one Adam step (torch.optim.Adam defaults: no weight
+ *      decay) on the per-splat tensors points (N,3), normals (N,3), colors
+ *      (N,C), std_devs (N,2) (any may be NULL with its gradient), moments
+ *      packed in m and v (N*(3+3+C+2) floats each, zeroed before step 1), then
+ *      with project != 0 the reference's constraints: normals renormalised
+ *      (x / (|x| + 1e-4)) and std_devs clamped to [sd_lo, sd_hi]. ---- */
+int uds_image_loss(int kind, size_t n, const float* x, const float* y, float scale, float* loss, float* grad,
+                   void* stream);
+int uds_adam_splats(int N, float* points, const float* g_points, float* normals, const float* g_normals,
+                    float* colors, const float* g_colors, int C, float* std_devs, const float* g_std_devs, float* m,
+                    float* v, int step, float lr, float beta1, float beta2, float eps, float sd_lo, float sd_hi,
+                    int project, void* stream);
+
 /* ---- proposal network (no counterpart in the reference).  Tensor-core
  *      kernels (tcgen05, accumulators in tensor memory). ---- */
 /* Layout check of the tensor-core path (debug): C (128 x N, fp32) =

@@ -73,6 +73,10 @@ _SIGS = {
     "uds_nearest_workspace_size": (c_size_t, [c_int, c_int, c_int, c_int, c_int]),
     "uds_nearest_samples": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_int,
                                     c_void_p, c_void_p, c_size_t, c_void_p]),
+    "uds_image_loss": (c_int, [c_int, c_size_t, c_void_p, c_void_p, c_float, c_void_p, c_void_p, c_void_p]),
+    "uds_adam_splats": (c_int, [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p,
+                                c_void_p, c_void_p, c_void_p, c_int, c_float, c_float, c_float, c_float, c_float,
+                                c_float, c_int, c_void_p]),
     "uds_splat_workspace_size": (c_size_t, [c_int, c_int]),
     "uds_splat_forward": (c_int, [c_int, c_int, c_int, c_int, c_float, c_void_p, c_void_p, c_void_p, c_int,
                                   c_int, c_void_p, c_float, c_void_p, c_void_p, c_size_t, c_void_p]),
