@@ -124,7 +124,9 @@ int uds_sample_stochastic(const uds_sample_params* prm, const float* points, con
  * its exact path probabilities); fallback (B,W,H) uint8 and n_fallback[B]
  * report them (either may be NULL).  With mlp_params NULL every pixel uses
  * the stochastic sampler.  indices (B,W,H,K) int32 (-1: none), weights
- * (B,W,H,K) float32.  Workspace: uds_proposal_workspace_size. */
+ * (B,W,H,K) float32.  Workspace: uds_proposal_workspace_size.  With
+ * mlp_params the call synchronises with the stream every 8 tree levels to
+ * stop once every draw has reached a leaf. */
 size_t uds_proposal_workspace_size(const uds_sample_params* prm);
 int uds_sample_proposal(const uds_sample_params* prm, const float* points, const float* normals,
                         const float* std_devs, const float* h_override, const float* mlp_params, float ess_tau,

@@ -1169,67 +1169,119 @@ __global__ void __launch_bounds__(128, 3) k_sample(Tree T, const ViewState* vs, 
 // their upper paths, so the child masses of the last path are kept per depth
 // (node ids are unique, so a hit is exact).  A draw that meets two zero
 // masses, or is still above the leaves after kTrace levels, stays -1 / 0.
-__global__ void __launch_bounds__(128) k_stochastic(Tree T, const ViewState* vs, int W, int H, int K,
-                                                    float precision, uint64_t seed,
-                                                    const uint64_t* __restrict__ seed_ptr, uint32_t view,
-                                                    int* __restrict__ indices, float* __restrict__ probs,
-                                                    uds_view_stats* st, const unsigned char* __restrict__ mask,
-                                                    float* __restrict__ weights) {
+__global__ void __launch_bounds__(128, 3) k_stochastic(Tree T, const ViewState* vs, int W, int H, int K,
+                                                       float precision, uint64_t seed,
+                                                       const uint64_t* __restrict__ seed_ptr, uint32_t view,
+                                                       int* __restrict__ indices, float* __restrict__ probs,
+                                                       uds_view_stats* st, const unsigned char* __restrict__ mask,
+                                                       float* __restrict__ weights) {
+    // same warp layout and per-pixel mass cache as k_sample: one warp walks
+    // its 32 pixels' trees together, then every lane draws its K paths; the
+    // masses come from the cache, the per-depth cache of earlier draws, or a
+    // grouped evaluation by the lanes at the same node (all bit-identical to
+    // separate getWeight calls)
+    if (seed_ptr) seed = *seed_ptr;
+    __shared__ WalkStack s_walk[4];
+    const unsigned full = 0xffffffffu;
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     int i = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= W || j >= H) return;
-    if (seed_ptr) seed = *seed_ptr;
+    int tid = threadIdx.x + blockDim.x * threadIdx.y;
+    int warp = tid >> 5;
+    size_t pixel = (size_t)j + (size_t)H * i;
+    bool live = (i < W && j < H) && (!mask || mask[pixel]);
     T.n = vs->n;
     T.sq = vs->sq;
     int n = T.n;
     if (n == 0) return;
-    size_t pixel = (size_t)j + (size_t)H * i;
-    if (mask && !mask[pixel]) return;
     float qx = (float)i, qy = (float)j;
-    float m0 = fmaxf(0.0f, node_weight(T, 0, qx, qy));
-    if (m0 < precision) return;
-    int cn[kTrace];
-    float cm0[kTrace], cm1[kTrace];
-    for (int d = 0; d < kTrace; ++d) cn[d] = -1;
-    int* out = indices + (size_t)K * pixel;
-    float* pq = probs + (size_t)K * pixel;
+    MassCache mc;
+    float m0;
+    warp_root_walk(T, qx, qy, live, mc, m0, s_walk[warp]);
+    m0 = fmaxf(0.0f, m0);
+    bool act = live && !(m0 < precision);
+    if (!__any_sync(full, act)) return;
+    int cv[kTrace];
+    float cw0[kTrace], cw1[kTrace];
+    int cvn = 0;
     bool overflow = false;
     for (int k = 0; k < K; ++k) {
         int v = 0, d = 0;
+        int e = (mc.ok && mc.m > 0) ? 0 : -1;
         float prob = 1.0f;
         uint32_t c[4];
-        bool ok = true;
-        while (v < n - 1) {
-            if ((d & 3) == 0) {
-                c[0] = (uint32_t)pixel; c[1] = view; c[2] = 0x80000000u | ((uint32_t)k << 8) | (uint32_t)(d >> 2);
-                c[3] = 0;
-                philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+        bool ok = act;
+        int4 L = T.lnk[0];
+        bool going = act && v < n - 1;
+        while (__any_sync(full, going)) {
+            int a = L.x, b = L.y;
+            float w0 = 0.0f, w1 = 0.0f;
+            int ea = -1, eb = -1;
+            bool need = false;
+            if (going) {
+                if (e >= 0) {
+                    if (e + 1 < mc.m && mc.node[e + 1] == a) ea = e + 1;
+                    int ib = ea >= 0 ? mc.skip[ea] : e + 1;
+                    if (ib < mc.m && mc.node[ib] == b) eb = ib;
+                }
+                if (d < cvn && cv[d] == v) {
+                    w0 = cw0[d];
+                    w1 = cw1[d];
+                } else if (ea >= 0 && eb >= 0) {
+                    w0 = fmaxf(0.0f, mc.mass[ea]);
+                    w1 = fmaxf(0.0f, mc.mass[eb]);
+                } else {
+                    need = true;
+                }
             }
-            float u = bits_to_uniform(c[d & 3]);
-            int4 L = T.lnk[v];
-            float w0, w1;
-            if (cn[d] == v) {
-                w0 = cm0[d];
-                w1 = cm1[d];
-            } else {
-                w0 = fmaxf(0.0f, node_weight(T, L.x, qx, qy));
-                w1 = fmaxf(0.0f, node_weight(T, L.y, qx, qy));
-                cn[d] = v;
-                cm0[d] = w0;
-                cm1[d] = w1;
+            unsigned pend = __ballot_sync(full, need);
+            while (pend) {
+                int leader = __ffs(pend) - 1;
+                int vv = __shfl_sync(full, v, leader);
+                bool mineg = need && v == vv;
+                unsigned grp = __ballot_sync(full, mineg);
+                if (mineg) {
+                    w0 = fmaxf(0.0f, ea >= 0 ? mc.mass[ea] : node_weight(T, a, qx, qy));
+                    w1 = fmaxf(0.0f, eb >= 0 ? mc.mass[eb] : node_weight(T, b, qx, qy));
+                }
+                pend &= ~grp;
             }
-            float sum = fadd(fadd(0.0f, w0), w1);
-            if (!(sum > 0.0f)) { ok = false; break; }
-            float r0 = fdiv(w0, sum);
-            if (u <= r0) { prob = fmul(prob, r0); v = L.x; }
-            else { prob = fmul(prob, fdiv(w1, sum)); v = L.y; }
-            if (++d >= kTrace && v < n - 1) { ok = false; overflow = true; break; }
+            if (going) {
+                cv[d] = v;
+                cw0[d] = w0;
+                cw1[d] = w1;
+                if (d >= cvn) cvn = d + 1;
+                if ((d & 3) == 0) {
+                    c[0] = (uint32_t)pixel; c[1] = view; c[2] = 0x80000000u | ((uint32_t)k << 8) | (uint32_t)(d >> 2);
+                    c[3] = 0;
+                    philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+                }
+                float u = bits_to_uniform(c[d & 3]);
+                float sum = fadd(fadd(0.0f, w0), w1);
+                if (!(sum > 0.0f)) {
+                    ok = false;
+                    going = false;
+                } else {
+                    float r0 = fdiv(w0, sum);
+                    if (u <= r0) { prob = fmul(prob, r0); v = a; e = ea; }
+                    else { prob = fmul(prob, fdiv(w1, sum)); v = b; e = eb; }
+                    ++d;
+                    if (d >= kTrace && v < n - 1) {
+                        ok = false;
+                        overflow = true;
+                        going = false;
+                    } else {
+                        L = T.lnk[v];
+                        going = v < n - 1;
+                    }
+                }
+            }
         }
         if (ok) {
-            out[k] = T.leaf_id[v - (n - 1)];
-            pq[k] = prob;
+            size_t o = (size_t)K * pixel + k;
+            indices[o] = T.leaf_id[v - (n - 1)];
+            probs[o] = prob;
             // importance weight of the draw: (leaf mass / root mass) / q
-            if (weights) weights[(size_t)K * pixel + k] = hermite_eval(T, v, T.cen[v], qx, qy) / m0 / prob;
+            if (weights) weights[o] = hermite_eval(T, v, T.cen[v], qx, qy) / m0 / prob;
         }
     }
     if (overflow) atomicAdd(&st->overflow, 1);
@@ -1342,14 +1394,24 @@ __global__ void k_prop_init(Tree T, const ViewState* vs, int W, int H, int K, fl
                             float* __restrict__ root_mass, int* __restrict__ node_out, int* __restrict__ draw_out,
                             float* __restrict__ logq_out, int* __restrict__ count_out, int* __restrict__ indices,
                             float* __restrict__ weights) {
+    // root masses by the warp-cooperative walk of k_sample (128-thread
+    // blocks, warps of consecutive threads)
+    __shared__ WalkStack s_walk[4];
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     int i = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= W || j >= H) return;
+    int warp = (threadIdx.x + blockDim.x * threadIdx.y) >> 5;
+    bool live = i < W && j < H;
     T.n = vs->n;
     T.sq = vs->sq;
     size_t pixel = (size_t)j + (size_t)H * i;
     float qx = (float)i, qy = (float)j;
-    float m0 = T.n > 0 ? fmaxf(0.0f, node_weight(T, 0, qx, qy)) : 0.0f;
+    float m0 = 0.0f;
+    if (T.n > 0) {
+        MassCache mc;
+        warp_root_walk(T, qx, qy, live, mc, m0, s_walk[warp]);
+        m0 = fmaxf(0.0f, m0);
+    }
+    if (!live) return;
     root_mass[pixel] = m0;
     if (T.n == 0 || m0 < precision) return;
     if (T.n == 1) {  // the root is the only leaf
@@ -1662,7 +1724,7 @@ extern "C" int uds_sample_stochastic(const uds_sample_params* prm, const float* 
     if (e == cudaSuccess) e = cudaMemsetAsync(probs, 0, sizeof(float) * per_view * prm->B, s);
     if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
     Tree T = tree_of(w);
-    dim3 block(16, 8);
+    dim3 block(8, 16);
     dim3 grid(cdiv(prm->H, block.x), cdiv(prm->W, block.y));
     for (int b = 0; b < prm->B; ++b) {
         if ((st = build_view(prm, w, b, points, normals, std_devs, h_override, s))) return st;
@@ -1840,12 +1902,19 @@ extern "C" int uds_sample_proposal(const uds_sample_params* prm, const float* po
         if (mlp_params) {
             e = cudaMemsetAsync(q.counts, 0, 16, s);
             if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
-            k_prop_init<<<grid, block, 0, s>>>(T, w.vs, prm->W, prm->H, prm->K, prm->precision, q.root_mass,
+            k_prop_init<<<dim3(cdiv(prm->H, 8), cdiv(prm->W, 16)), dim3(8, 16), 0, s>>>(T, w.vs, prm->W, prm->H, prm->K, prm->precision, q.root_mass,
                                                q.node[0], q.draw[0], q.logq[0], q.counts, idx, wt);
             if ((st = launch_status())) return st;
             unsigned nb = cdiv(per_view, 256);
             int cur = 0;
             for (int level = 0; level < kTrace; ++level) {
+                if (level % 8 == 7) {  // stop once every draw has reached its leaf
+                    int left = 0;
+                    e = cudaMemcpyAsync(&left, q.counts + cur, sizeof(int), cudaMemcpyDeviceToHost, s);
+                    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+                    if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
+                    if (left == 0) break;
+                }
                 k_prop_features<<<nb, 256, 0, s>>>(T, w.vs, prm->H, prm->K, level, q.counts + cur, q.node[cur],
                                                    q.draw[cur], q.X);
                 if ((st = launch_status())) return st;
