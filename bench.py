@@ -72,6 +72,18 @@ def dist_info():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def replica_max(t, world, device):
+    """The slowest rank's time (every rank gets it); replicas run the same
+    workload independently, so the job's throughput is world * units / max."""
+    if world <= 1:
+        return float(t)
+    import torch
+    import torch.distributed as dist
+    tt = torch.tensor([float(t)], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons, streamed every 50 ms by one
     nvidia-smi process (-lms) for the duration of the timed region."""
@@ -588,10 +600,7 @@ def main():
     t_eager = t_step
     if graph is not None:
         t_eager = float(np.mean(timed_steps(max(3, args.steps // 2), False)))
-    if world > 1:
-        tt = torch.tensor([t_step], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step = float(tt.item())
+    t_step = replica_max(t_step, world, dev)
     value = world * S / (t_step * 1e-3) / 1e6
 
     # ---- e2e: host buffers, H2D of every input and D2H of the loss per step
@@ -615,10 +624,7 @@ def main():
 
     t_e2e = e2e_steps(max(2, args.steps // 2), graph is not None)
     t_e2e_eager = e2e_steps(max(2, args.steps // 2), False) if graph is not None else t_e2e
-    if world > 1:
-        tt = torch.tensor([t_e2e], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_e2e = float(tt.item())
+    t_e2e = replica_max(t_e2e, world, dev)
     e2e = world * S / t_e2e / 1e6
 
     # ---- roofline of the dominant kernel: the per-pixel descent alone

@@ -270,3 +270,26 @@ def test_pixel_scatter_gather_oracle():
         assert np.all(s[b][~m] == 0)
     gt = oracle.pixel_gather(idx, g, N)
     assert abs(float((s * g).sum()) - float((v * gt).sum())) < 1e-4
+
+
+def test_nearest_samples_oracle_brute_force():
+    """The oracle's nearest-sample lists against a direct numpy restatement
+    (surface = first largest weight; candidates ranked by (distance, index))."""
+    rng = np.random.default_rng(12)
+    B, W, H, K, N, M = 1, 9, 7, 5, 40, 4
+    idx = rng.integers(-1, N, size=(B, W, H, K)).astype(np.int32)
+    w = rng.random((B, W, H, K)).astype(np.float32)
+    pts = rng.normal(size=(1, N, 3)).astype(np.float32)
+    got = oracle.nearest_samples(idx, w, pts, M)
+    cands = {s: set() for s in range(N)}
+    for pix_i, pix_w in zip(idx.reshape(-1, K), w.reshape(-1, K)):
+        s = int(pix_i[int(np.argmax(pix_w))])
+        if s < 0:
+            continue
+        cands[s] |= {int(c) for c in pix_i if c >= 0 and c != s}
+    p = pts[0].astype(np.float32)
+    for s in range(N):
+        d = sorted((float(np.float32(np.sqrt(np.float32(np.sum(np.square(p[s] - p[c], dtype=np.float32)))))), c)
+                   for c in cands[s])
+        want = [c for _, c in d[:M]] + [-1] * max(0, M - len(d))
+        assert list(got[s]) == want, (s, list(got[s]), want)
