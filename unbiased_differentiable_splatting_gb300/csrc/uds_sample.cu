@@ -26,6 +26,8 @@
 // intrinsic (or is an IEEE-exact library op: sqrt, division, fma), so the
 // Morton keys, the tree, the FGT masses and the sampled indices equal the CPU
 // oracle's bit for bit given the same inputs and uniforms.
+#include <mutex>
+
 #include "uds_ewa.cuh"
 
 namespace uds {
@@ -1658,6 +1660,41 @@ static int check_params(const uds_sample_params* p) {
 
 using namespace uds;
 
+namespace uds {
+// Side streams for building several views' trees at once (their workspace
+// slots are disjoint).  Created per device on first use outside stream
+// capture; a call under capture before that builds the views in order.
+constexpr int kBuildStreams = 4;
+struct BuildStreams {
+    bool ready = false;
+    std::mutex enqueue;  // one call at a time forks, builds and joins
+    cudaStream_t side[kBuildStreams];
+    cudaEvent_t fork, join[kBuildStreams];
+};
+
+static BuildStreams* build_streams(cudaStream_t s) {
+    static std::mutex mu;
+    static BuildStreams pool[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lock(mu);
+    BuildStreams& b = pool[dev];
+    if (b.ready) return &b;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) return nullptr;
+    bool ok = cudaEventCreateWithFlags(&b.fork, cudaEventDisableTiming) == cudaSuccess;
+    for (int k = 0; k < kBuildStreams && ok; ++k)
+        ok = cudaStreamCreateWithFlags(&b.side[k], cudaStreamNonBlocking) == cudaSuccess &&
+             cudaEventCreateWithFlags(&b.join[k], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    b.ready = true;
+    return &b;
+}
+}  // namespace uds
+
 // uds_sample keeps every view's tree resident (one slot per view) so that one
 // descent launch covers all views; the other entry points use slot 0.
 extern "C" size_t uds_sample_workspace_size(const uds_sample_params* prm) {
@@ -1680,11 +1717,29 @@ extern "C" int uds_sample(const uds_sample_params* prm, const float* points, con
     size_t per_view = (size_t)prm->W * prm->H * prm->K;
     cudaError_t e = cudaMemsetAsync(indices, 0xFF, sizeof(int32_t) * per_view * prm->B, s);
     if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
-    // every view's tree in its own slot (the per-view record stays in slot 0)
+    // every view's tree in its own slot (the per-view record stays in slot 0);
+    // several views at once on side streams forked from and joined to s
+    BuildStreams* bs = prm->B > 1 ? build_streams(s) : nullptr;
+    int nside = bs ? (prm->B < kBuildStreams ? prm->B : kBuildStreams) : 0;
+    std::unique_lock<std::mutex> hold;
+    if (nside) hold = std::unique_lock<std::mutex>(bs->enqueue);
+    if (nside) {
+        e = cudaEventRecord(bs->fork, s);
+        for (int k = 0; k < nside && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(bs->side[k], bs->fork, 0);
+        if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
+    }
     for (int b = 0; b < prm->B; ++b) {
         Ws wb = layout(prm, base + slot * (size_t)b);
         wb.stats = w.stats;
-        if ((st = build_view(prm, wb, b, points, normals, std_devs, h_override, s))) return st;
+        cudaStream_t sb = nside ? bs->side[b % nside] : s;
+        if ((st = build_view(prm, wb, b, points, normals, std_devs, h_override, sb))) return st;
+    }
+    if (nside) {
+        for (int k = 0; k < nside && e == cudaSuccess; ++k) {
+            e = cudaEventRecord(bs->join[k], bs->side[k]);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(s, bs->join[k], 0);
+        }
+        if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
     }
     if (prm->N > 0) {
         // one descent launch over all views
