@@ -223,6 +223,13 @@ int uds_mlp_forward(int R, const float* X, const float* params, float* logits, i
 /* Same, the row count read on the device from *R_dev (at most R_max rows). */
 int uds_mlp_forward_dev(int R_max, const int* R_dev, const float* X, const float* params, float* logits, int* err,
                         void* stream);
+/* Same, the rows given as bf16 in the network's operand layout: row r is in
+ * 128-row tile r/128 (4096 bytes at X_tiles + 4096*(r/128); element (r%128,
+ * k) at byte (r%128/8)*256 + (k/8)*128 + (r%8)*16 + (k%8)*2), the buffer
+ * holding ceil(R_max/128) tiles, 16-byte aligned.  Tiles are streamed by bulk
+ * copies. */
+int uds_mlp_forward_tiles(int R_max, const int* R_dev, const void* X_tiles, const float* params, float* logits,
+                          int* err, void* stream);
 /* Training: adds the gradient of the mean cross-entropy between
  * softmax(logits) and (target, 1 - target) over the R rows to grad (fp32,
  * uds_mlp_param_count() entries, zeroed by the caller) and the mean loss to

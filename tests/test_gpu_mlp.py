@@ -147,3 +147,38 @@ def test_mlp_training_reduces_loss(L):
     # entropy floor of the soft targets
     floor = float(-(target * target.log() + (1 - target) * (1 - target).log()).mean())
     assert losses[1] - floor < 0.25 * (losses[0] - floor), (losses, floor)
+
+
+def pack_tiles(X):
+    """Rows (R,16) -> bf16 operand tiles (128 rows x 16 per 4096 bytes)."""
+    R = X.shape[0]
+    tiles = (R + 127) // 128
+    buf = torch.zeros(tiles * 2048, dtype=torch.bfloat16, device=X.device)
+    r = torch.arange(R, device=X.device)[:, None]
+    k = torch.arange(16, device=X.device)[None, :]
+    rr = r % 128
+    idx = (r // 128) * 2048 + (rr // 8) * 128 + (k // 8) * 64 + (rr % 8) * 8 + (k % 8)
+    buf[idx.reshape(-1)] = X.to(torch.bfloat16).reshape(-1)
+    return buf
+
+
+@pytest.mark.parametrize("R,Rdev", [(1, 1), (1000, 1000), (70001, 70001), (70001, 12345)])
+def test_mlp_forward_tiles_bulk_copy(L, R, Rdev):
+    """The bulk-copy (TMA engine) variant on pre-laid-out bf16 tiles gives the
+    same logits as the fp32-row variant, for the device-side row count."""
+    n = L.uds_mlp_param_count()
+    P = init_params(n, seed=R).to(DEV)
+    X = (torch.randn(R, 16, generator=torch.Generator().manual_seed(2)) * 2).to(DEV)
+    s = torch.cuda.current_stream().cuda_stream
+    err = torch.zeros(1, dtype=torch.int32, device=DEV)
+    ref = torch.full((R, 2), float("nan"), device=DEV)
+    assert L.uds_mlp_forward(R, X.data_ptr(), P.data_ptr(), ref.data_ptr(), err.data_ptr(), s) == 0
+    tiles = pack_tiles(X)
+    cnt = torch.tensor([Rdev], dtype=torch.int32, device=DEV)
+    out = torch.full((R, 2), float("nan"), device=DEV)
+    assert L.uds_mlp_forward_tiles(R, cnt.data_ptr(), tiles.data_ptr(), P.data_ptr(), out.data_ptr(),
+                                   err.data_ptr(), s) == 0
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    assert torch.equal(out[:Rdev], ref[:Rdev])
+    assert torch.isnan(out[Rdev:]).all()

@@ -60,6 +60,7 @@ _SIGS = {
     "uds_mlp_adam": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_float, c_float, c_float, c_float,
                              c_void_p]),
     "uds_mlp_forward_dev": (c_int, [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "uds_mlp_forward_tiles": (c_int, [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "uds_proposal_workspace_size": (c_size_t, [ctypes.POINTER(SampleParams)]),
     "uds_sample_proposal": (c_int, [ctypes.POINTER(SampleParams), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                     c_float, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,

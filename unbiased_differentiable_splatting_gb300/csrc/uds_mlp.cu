@@ -248,6 +248,129 @@ __global__ void __launch_bounds__(128) k_mlp_forward(int R, const int* __restric
     if (warp == 0) tc::tmem_dealloc(taddr, 64);
 }
 
+// Inference on feature rows already in the tensor-core operand layout: row r
+// is in 128-row tile r / 128, whose 4096 bytes (bf16, K-major core layout)
+// start at Xt + 4096 * (r / 128).  Tiles stream into shared memory by bulk
+// copies (the TMA engine) completing on per-buffer mbarriers, two buffers
+// deep: tile i + 1 is in flight while tile i runs its four layers.
+struct MlpTileSmem {
+    __align__(1024) unsigned char w1[mlp::kHid * mlp::kIn * 2];
+    __align__(1024) unsigned char w2[mlp::kHid * mlp::kHid * 2];
+    __align__(1024) unsigned char w3[mlp::kHid * mlp::kHid * 2];
+    __align__(1024) unsigned char w4[mlp::kOut * mlp::kHid * 2];
+    __align__(1024) unsigned char x[2][mlp::kTile * mlp::kIn * 2];
+    __align__(1024) unsigned char h[mlp::kTile * mlp::kHid * 2];
+    float bias[3 * mlp::kHid + mlp::kOut];
+    uint64_t mbar;      // MMA completion
+    uint64_t xbar[2];   // tile arrivals
+    uint32_t taddr;
+};
+
+constexpr uint32_t kTileBytes = mlp::kTile * mlp::kIn * 2;
+
+__global__ void __launch_bounds__(128) k_mlp_forward_tiles(int R, const int* __restrict__ Rdev,
+                                                           const unsigned char* __restrict__ Xt,
+                                                           const float* __restrict__ P, float* __restrict__ out,
+                                                           int* __restrict__ err) {
+    if (Rdev) R = min(R, *Rdev);
+    if ((int)blockIdx.x * mlp::kTile >= R) return;
+    extern __shared__ __align__(1024) unsigned char s_raw[];
+    MlpTileSmem& S = *reinterpret_cast<MlpTileSmem*>(s_raw);
+    using namespace mlp;
+    int tid = threadIdx.x, warp = tid >> 5;
+    int tiles = (R + kTile - 1) / kTile;
+    if (tid == 0) {
+        tc::mbar_init(&S.mbar, 1);
+        tc::mbar_init(&S.xbar[0], 1);
+        tc::mbar_init(&S.xbar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        // first tile on its way while the weights are staged
+        tc::mbar_expect_tx(&S.xbar[0], kTileBytes);
+        tc::bulk_load(S.x[0], Xt + (size_t)blockIdx.x * kTileBytes, kTileBytes, &S.xbar[0]);
+    }
+    stage_matrix(S.w1, P + oW1, kHid, kIn);
+    stage_matrix(S.w2, P + oW2, kHid, kHid);
+    stage_matrix(S.w3, P + oW3, kHid, kHid);
+    stage_matrix(S.w4, P + oW4, kOut, kHid);
+    for (int i = tid; i < kHid; i += 128) {
+        S.bias[i] = P[oB1 + i];
+        S.bias[kHid + i] = P[oB2 + i];
+        S.bias[2 * kHid + i] = P[oB3 + i];
+    }
+    if (tid < kOut) S.bias[3 * kHid + tid] = P[oB4 + tid];
+    if (warp == 0) {
+        tc::tmem_alloc(&S.taddr, 64);
+        tc::tmem_relinquish();
+    }
+    tc::fence_before_sync();
+    tc::fence_async_smem();
+    __syncthreads();
+    tc::fence_after_sync();
+    uint32_t taddr = S.taddr;
+    uint32_t lane_base = taddr + ((uint32_t)(warp * 32) << 16);
+    uint32_t phase = 0, xphase[2] = {0u, 0u};
+    bool pending[2] = {true, false};  // thread 0's view of the loads in flight
+    bool ok = true;
+    int it = 0;
+    for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x, ++it) {
+        int b = it & 1;
+        int tn = t + gridDim.x;
+        // the other buffer was read by the previous tile's first layer, which
+        // has completed: refill it with the next tile
+        if (tid == 0 && tn < tiles) {
+            tc::mbar_expect_tx(&S.xbar[b ^ 1], kTileBytes);
+            tc::bulk_load(S.x[b ^ 1], Xt + (size_t)tn * kTileBytes, kTileBytes, &S.xbar[b ^ 1]);
+            pending[b ^ 1] = true;
+        }
+        bool got = tc::mbar_wait(&S.xbar[b], xphase[b] & 1u, kWaitLimit);
+        ++xphase[b];
+        pending[b] = false;
+        ok = __syncthreads_and(got) != 0;
+        if (!ok) break;
+        const unsigned char* a = S.x[b];
+        int K = kIn;
+        const unsigned char* ws[3] = {S.w1, S.w2, S.w3};
+        for (int l = 0; l < 3 && ok; ++l) {
+            ok = mlp_layer(taddr, a, ws[l], K, kHid, &S.mbar, phase);
+            if (!ok) break;
+            for (int c0 = 0; c0 < kHid; c0 += 16) {
+                float v[16];
+                tc::tmem_ld16(lane_base + (uint32_t)c0, v);
+#pragma unroll
+                for (int c = 0; c < 16; ++c) v[c] = fmaxf(v[c] + S.bias[l * kHid + c0 + c], 0.0f);
+                put8_bf16(S.h, tid, c0, kHid, v);
+                put8_bf16(S.h, tid, c0 + 8, kHid, v + 8);
+            }
+            tc::fence_before_sync();
+            tc::fence_async_smem();
+            __syncthreads();
+            a = S.h;
+            K = kHid;
+        }
+        if (!ok) break;
+        ok = mlp_layer(taddr, S.h, S.w4, kHid, kOut, &S.mbar, phase);
+        if (!ok) break;
+        float v[16];
+        tc::tmem_ld16(lane_base, v);
+        int row = t * kTile + tid;
+        if (row < R) {
+            out[(size_t)row * kLogits] = v[0] + S.bias[3 * kHid];
+            out[(size_t)row * kLogits + 1] = v[1] + S.bias[3 * kHid + 1];
+        }
+        tc::fence_before_sync();
+        __syncthreads();
+    }
+    if (!ok && (tid & 31) == 0) atomicExch(err, 1);
+    // a tile load still in flight (after an error) must land before exit
+    if (tid == 0 && !ok) {
+        for (int q = 0; q < 2; ++q)
+            if (pending[q]) tc::mbar_wait(&S.xbar[q], xphase[q] & 1u, kWaitLimit);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(taddr, 64);
+}
+
 // ------------------------------------------------------------ training
 // Gradient of the mean cross-entropy between the branch distribution
 // softmax(logits) and the target (p, 1 - p) over R rows, added to G (fp32,
@@ -620,5 +743,30 @@ extern "C" int uds_mlp_adam(float* params, float* grad, float* m1, float* m2, in
     float c1 = 1.0f - powf(beta1, (float)step), c2 = 1.0f - powf(beta2, (float)step);
     k_mlp_adam<<<cdiv(mlp::kParams, 256), 256, 0, as_stream(stream)>>>(params, grad, m1, m2, lr, beta1, beta2, eps,
                                                                       c1, c2);
+    return launch_status();
+}
+
+// Feature rows given as bf16 tiles in the operand layout (uds_sample's
+// proposal descent writes them so); the row count is read on the device.
+extern "C" int uds_mlp_forward_tiles(int R_max, const int* R_dev, const void* X_tiles, const float* params,
+                                     float* logits, int* err, void* stream) {
+    using namespace uds;
+    if (R_max < 0 || (R_max > 0 && (!X_tiles || !params || !logits)) || !err) return UDS_ERR_ARGUMENT;
+    if ((reinterpret_cast<uintptr_t>(X_tiles) & 15) != 0) return UDS_ERR_ARGUMENT;
+    if (R_max == 0) return UDS_OK;
+    static bool attr = false;
+    size_t smem = sizeof(MlpTileSmem) + 1024;
+    if (!attr) {
+        cudaFuncSetAttribute(k_mlp_forward_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr = true;
+    }
+    int tiles = (R_max + mlp::kTile - 1) / mlp::kTile;
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int grid = tiles < 4 * sms ? tiles : 4 * sms;
+    k_mlp_forward_tiles<<<grid, 128, smem, as_stream(stream)>>>(R_max, R_dev,
+                                                               reinterpret_cast<const unsigned char*>(X_tiles),
+                                                               params, logits, err);
     return launch_status();
 }

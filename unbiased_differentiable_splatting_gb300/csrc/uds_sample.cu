@@ -28,7 +28,10 @@
 // oracle's bit for bit given the same inputs and uniforms.
 #include <mutex>
 
+#include <cuda_bf16.h>
+
 #include "uds_ewa.cuh"
+#include "uds_tc.cuh"
 
 namespace uds {
 
@@ -1431,9 +1434,12 @@ __global__ void k_prop_init(Tree T, const ViewState* vs, int W, int H, int K, fl
     }
 }
 
+// Rows go straight into the network's operand layout: bf16, 128-row tiles of
+// 4096 bytes, K-major core matrices (two 16-byte stores per row), so the
+// network kernel can stream whole tiles with bulk copies.
 __global__ void k_prop_features(Tree T, const ViewState* vs, int H, int K, int level, const int* __restrict__ count,
                                 const int* __restrict__ node_in, const int* __restrict__ draw_in,
-                                float* __restrict__ X) {
+                                unsigned char* __restrict__ Xt) {
     int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= *count) return;
     T.n = vs->n;
@@ -1442,8 +1448,14 @@ __global__ void k_prop_features(Tree T, const ViewState* vs, int H, int K, int l
     float qx = (float)(pixel / H), qy = (float)(pixel % H);
     float f[kFeat];
     branch_features(T, node_in[r], level, qx, qy, f);
+    unsigned char* tile = Xt + (size_t)(r >> 7) * (128 * kFeat * 2);
 #pragma unroll
-    for (int q = 0; q < kFeat; ++q) X[(size_t)r * kFeat + q] = f[q];
+    for (int c = 0; c < kFeat; c += 8) {
+        __nv_bfloat162 h[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) h[q] = __floats2bfloat162_rn(f[c + 2 * q], f[c + 2 * q + 1]);
+        *reinterpret_cast<uint4*>(tile + tc::kmajor_offset(r & 127, c, kFeat)) = *reinterpret_cast<uint4*>(h);
+    }
 }
 
 // Take one branch per draw with the network's q; finished draws write their
@@ -1884,8 +1896,8 @@ extern "C" int uds_fgt_eval(const uds_sample_params* prm, int m, const int32_t* 
     return launch_status();
 }
 
-extern "C" int uds_mlp_forward_dev(int R_max, const int* R_dev, const float* X, const float* params, float* logits,
-                                   int* err, void* stream);
+extern "C" int uds_mlp_forward_tiles(int R_max, const int* R_dev, const void* X_tiles, const float* params,
+                                     float* logits, int* err, void* stream);
 
 namespace uds {
 // Proposal-mode buffers after the tree slot.
@@ -1913,7 +1925,8 @@ static PropWs prop_layout(const uds_sample_params* p, char* base) {
         q.draw[c] = (int*)take(4 * D);
         q.logq[c] = (float*)take(4 * D);
     }
-    q.X = (float*)take(4 * kFeat * D);
+    // feature tiles: 128 rows of 16 bf16 per 4096 bytes
+    q.X = (float*)take(cdiv(D > 0 ? D : 1, 128) * (size_t)4096);
     q.logits = (float*)take(8 * D);
     q.counts = (int*)take(16);
     q.bytes = off;
@@ -1971,10 +1984,10 @@ extern "C" int uds_sample_proposal(const uds_sample_params* prm, const float* po
                     if (left == 0) break;
                 }
                 k_prop_features<<<nb, 256, 0, s>>>(T, w.vs, prm->H, prm->K, level, q.counts + cur, q.node[cur],
-                                                   q.draw[cur], q.X);
+                                                   q.draw[cur], reinterpret_cast<unsigned char*>(q.X));
                 if ((st = launch_status())) return st;
-                if ((st = uds_mlp_forward_dev((int)per_view, q.counts + cur, q.X, mlp_params, q.logits, q.counts + 3,
-                                              stream)))
+                if ((st = uds_mlp_forward_tiles((int)per_view, q.counts + cur, q.X, mlp_params, q.logits,
+                                                q.counts + 3, stream)))
                     return st;
                 e = cudaMemsetAsync(q.counts + (cur ^ 1), 0, 4, s);
                 if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
