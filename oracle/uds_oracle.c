@@ -1061,13 +1061,23 @@ orc_tree* orc_tree_build(int W, int H, float f, int N, const float* pts, float h
      * deterministic flavour (the GPU's arithmetic) builds t_a = s^a / a! by
      * the recurrence t_a = (t_{a-1} * s) / a and adds fma(tx_a, ty_b, C_ab). */
     float sq = sqrtf(2.0f * h * h);
+    float isq = 1.0f / sq;
+    static const float inv_int[ORC_MAXDEGREE + 1] = {0.0f, 1.0f / 1, 1.0f / 2, 1.0f / 3, 1.0f / 4, 1.0f / 5,
+                                                     1.0f / 6, 1.0f / 7, 1.0f / 8, 1.0f / 9, 1.0f / 10, 1.0f / 11,
+                                                     1.0f / 12, 1.0f / 13, 1.0f / 14, 1.0f / 15, 1.0f / 16};
     for (int v = 0; v < L0; ++v) {
         int p = t->degree[v];
         if (p < 0) continue;
         float* C = &t->coef[t->offset[v]];
         for (int i = t->first[v]; i <= t->last[v]; ++i) {
-            float s0 = (t->leafxy[2 * i] - t->centre[2 * v]) / sq;
-            float s1 = (t->leafxy[2 * i + 1] - t->centre[2 * v + 1]) / sq;
+            float s0, s1;
+            if (fl == ORC_LIBM) {
+                s0 = (t->leafxy[2 * i] - t->centre[2 * v]) / sq;
+                s1 = (t->leafxy[2 * i + 1] - t->centre[2 * v + 1]) / sq;
+            } else {
+                s0 = (t->leafxy[2 * i] - t->centre[2 * v]) * isq;
+                s1 = (t->leafxy[2 * i + 1] - t->centre[2 * v + 1]) * isq;
+            }
             if (fl == ORC_LIBM) {
                 for (int x = 0; x <= p; ++x)
                     for (int y = 0; y <= p; ++y) {
@@ -1079,8 +1089,8 @@ orc_tree* orc_tree_build(int W, int H, float f, int N, const float* pts, float h
                 tx[0] = 1.0f;
                 ty[0] = 1.0f;
                 for (int a = 1; a <= p; ++a) {
-                    tx[a] = (tx[a - 1] * s0) / (float)a;
-                    ty[a] = (ty[a - 1] * s1) / (float)a;
+                    tx[a] = (tx[a - 1] * s0) * inv_int[a];
+                    ty[a] = (ty[a - 1] * s1) * inv_int[a];
                 }
                 for (int x = 0; x <= p; ++x)
                     for (int y = 0; y <= p; ++y) C[x * (p + 1) + y] = fmaf(tx[x], ty[y], C[x * (p + 1) + y]);
@@ -1114,8 +1124,15 @@ void orc_tree_export(const orc_tree* t, unsigned* keys, int* ids, int* left, int
 /* evluateHermite (hermitefmm.cuh:213-237) with hermiteFunction (:35-47) */
 static float hermite_eval(const orc_tree* t, int v, const float* q, int fl) {
     float sq = sqrtf(2.0f * t->h * t->h);
-    float tx = (q[0] - t->centre[2 * v]) / sq;
-    float ty = (q[1] - t->centre[2 * v + 1]) / sq;
+    float tx, ty;
+    if (fl == ORC_LIBM) {  /* the reference divides */
+        tx = (q[0] - t->centre[2 * v]) / sq;
+        ty = (q[1] - t->centre[2 * v + 1]) / sq;
+    } else {  /* the deterministic flavour multiplies by 1 / sq */
+        float isq = 1.0f / sq;
+        tx = (q[0] - t->centre[2 * v]) * isq;
+        ty = (q[1] - t->centre[2 * v + 1]) * isq;
+    }
     int p = t->degree[v];
     float hx[ORC_MAXDEGREE + 1], hy[ORC_MAXDEGREE + 1];
     float ex = xexpf(-(tx * tx), fl), ey = xexpf(-(ty * ty), fl);

@@ -45,7 +45,8 @@ struct ViewState {            // per-view device scalars (lives in the workspace
     float h, radius, lo_x, hi_x, lo_y, hi_y, sq;  // sq = sqrt(2 h^2)
     int n;                    // visible splats
     unsigned coef_used;
-    int pad[5];
+    float isq;                // 1 / sq (the series' scaled offsets multiply by it)
+    int pad[4];
 };
 
 // ----------------------------------------------------------- workspace
@@ -175,6 +176,7 @@ __global__ void k_view_setup(const float* h_override, int view, float W, float H
     vs->lo_y = -r;
     vs->hi_y = fadd(H, r);
     vs->sq = fsqrt(fmul(fmul(2.0f, h), h));
+    vs->isq = fdiv(1.0f, vs->sq);
     vs->n = 0;
     vs->coef_used = 0;
     stats[view].h = h;
@@ -636,13 +638,17 @@ __global__ void k_assign(ViewState* vs, float4* cen, const uint32_t* __restrict_
 // ----------------------------------------------------------------- 7 P2M
 // shiftLeafHermiteExpansion (hermitefmm.cuh:119-138) summed per node over
 // its leaves in Morton order: C_ab = sum_i t_a(s0_i) t_b(s1_i) with
-// t_a(s) = s^a / a!, s = (leaf - centre) / sqrt(2 h^2).  One warp per
+// t_a(s) = s^a / a!, s = (leaf - centre) * (1 / sqrt(2 h^2)).  One warp per
 // internal node.  For a chunk of 32 leaves each lane builds one leaf's
-// t-tables in shared memory (t_a = (t_{a-1} s) / a); lane (g, b) then owns
+// t-tables in shared memory (t_a = (t_{a-1} s) * (1 / a)); lane (g, b) then owns
 // column b and rows a = g, g + G, ... (G = 32 / (p+1) row groups) and adds
 // fma(t_a(s0), t_b(s1), C_ab) leaf by leaf, so every coefficient is summed in
 // leaf order exactly as the oracle's deterministic flavour does.
 constexpr int kP2MWarps = 4;
+// 1 / a, rounded once at compile time (the oracle uses the same constants)
+__constant__ float kInvInt[kMaxDegree + 1] = {0.0f, 1.0f / 1, 1.0f / 2, 1.0f / 3, 1.0f / 4, 1.0f / 5, 1.0f / 6,
+                                              1.0f / 7, 1.0f / 8, 1.0f / 9, 1.0f / 10, 1.0f / 11, 1.0f / 12,
+                                              1.0f / 13, 1.0f / 14, 1.0f / 15, 1.0f / 16};
 constexpr int kTStride = kMaxDegree + 1;  // odd: conflict-free row writes
 
 __global__ void __launch_bounds__(32 * kP2MWarps) k_p2m(const ViewState* vs, const int4* __restrict__ lnk,
@@ -659,7 +665,7 @@ __global__ void __launch_bounds__(32 * kP2MWarps) k_p2m(const ViewState* vs, con
     if (p < 0) return;
     int off = meta_offset(c.w);
     int4 L = lnk[v];
-    float sq = vs->sq;
+    float isq = vs->isq;
     int P1 = p + 1;
     int G = 32 / P1;
     int b = lane % P1, g = lane / P1;
@@ -675,14 +681,14 @@ __global__ void __launch_bounds__(32 * kP2MWarps) k_p2m(const ViewState* vs, con
         int cnt = min(32, end - i0);
         if (lane < cnt) {
             float2 q = leaf_xy[i0 + lane];
-            float s0 = fdiv(fsub(q.x, c.x), sq);
-            float s1 = fdiv(fsub(q.y, c.y), sq);
+            float s0 = fmul(fsub(q.x, c.x), isq);
+            float s1 = fmul(fsub(q.y, c.y), isq);
             float ax = 1.0f, ay = 1.0f;
             tx[lane * kTStride] = 1.0f;
             ty[lane * kTStride] = 1.0f;
             for (int a = 1; a <= p; ++a) {
-                ax = fdiv(fmul(ax, s0), (float)a);
-                ay = fdiv(fmul(ay, s1), (float)a);
+                ax = fmul(fmul(ax, s0), kInvInt[a]);
+                ay = fmul(fmul(ay, s1), kInvInt[a]);
                 tx[lane * kTStride + a] = ax;
                 ty[lane * kTStride + a] = ay;
             }
@@ -720,18 +726,30 @@ struct Tree {
     const int* leaf_id;
     int n;
     float sq;
+    float isq;
 };
 
 // evluateHermite with hermiteFunction (hermitefmm.cuh:35-47, 213-237): the
 // Hermite functions follow the reference's recursion; the series is summed
 // row-factored, sum_a h_a(tx) (sum_b C_ab h_b(ty)), with fused multiply-adds
 // (the CPU oracle's deterministic flavour sums the same way).
-__device__ __forceinline__ float hermite_eval(const Tree& T, int v, float4 c, float qx, float qy) {
-    float tx = fdiv(fsub(qx, c.x), T.sq);
-    float ty = fdiv(fsub(qy, c.y), T.sq);
+// A leaf's expansion is its own Gaussian: degree 0, coefficient 1.  Callers
+// that know they hold a leaf use this directly, which keeps the series'
+// loops out of their code.
+__device__ __forceinline__ float leaf_mass(const Tree& T, float4 c, float qx, float qy) {
+    float tx = fmul(fsub(qx, c.x), T.isq);
+    float ty = fmul(fsub(qy, c.y), T.isq);
     float ex = det_expf(-fmul(tx, tx));
     float ey = det_expf(-fmul(ty, ty));
-    if (v >= T.n - 1) return fadd(0.0f, fmul(fmul(1.0f, ex), ey));
+    return fadd(0.0f, fmul(fmul(1.0f, ex), ey));
+}
+
+__device__ __forceinline__ float hermite_eval(const Tree& T, int v, float4 c, float qx, float qy) {
+    if (v >= T.n - 1) return leaf_mass(T, c, qx, qy);
+    float tx = fmul(fsub(qx, c.x), T.isq);
+    float ty = fmul(fsub(qy, c.y), T.isq);
+    float ex = det_expf(-fmul(tx, tx));
+    float ey = det_expf(-fmul(ty, ty));
     int p = meta_degree(c.w);
     const float* C = T.coef + meta_offset(c.w);
     float hy[kMaxDegree + 1];
@@ -987,6 +1005,7 @@ __global__ void __launch_bounds__(128, 3) k_sample(Tree T, const ViewState* vs, 
     bool live = (i < W && j < H);
     T.n = vs->n;
     T.sq = vs->sq;
+    T.isq = vs->isq;
     if (T.n == 0) return;  // indices were preset to -1 (uniform over the grid)
     size_t pixel = (size_t)j + (size_t)H * i;
     float qx = (float)i, qy = (float)j;
@@ -1139,7 +1158,7 @@ __global__ void __launch_bounds__(128, 3) k_sample(Tree T, const ViewState* vs, 
         for (int k = 0; k < KM; ++k) {
             if (k < cnt) {
                 int leafNode = T.n - 1 + f0 + k;
-                float pw = fmaxf(0.0f, hermite_eval(T, leafNode, T.cen[leafNode], qx, qy));
+                float pw = fmaxf(0.0f, leaf_mass(T, T.cen[leafNode], qx, qy));
                 float key = fdiv(u[k], pw);
                 int index = T.leaf_id[f0 + k];
                 bool done = false;
@@ -1196,6 +1215,7 @@ __global__ void __launch_bounds__(128, 3) k_stochastic(Tree T, const ViewState* 
     bool live = (i < W && j < H) && (!mask || mask[pixel]);
     T.n = vs->n;
     T.sq = vs->sq;
+    T.isq = vs->isq;
     int n = T.n;
     if (n == 0) return;
     float qx = (float)i, qy = (float)j;
@@ -1286,7 +1306,7 @@ __global__ void __launch_bounds__(128, 3) k_stochastic(Tree T, const ViewState* 
             indices[o] = T.leaf_id[v - (n - 1)];
             probs[o] = prob;
             // importance weight of the draw: (leaf mass / root mass) / q
-            if (weights) weights[o] = hermite_eval(T, v, T.cen[v], qx, qy) / m0 / prob;
+            if (weights) weights[o] = leaf_mass(T, T.cen[v], qx, qy) / m0 / prob;
         }
     }
     if (overflow) atomicAdd(&st->overflow, 1);
@@ -1315,7 +1335,7 @@ __device__ __forceinline__ float box_distance(float4 b, float qx, float qy) {
 
 __device__ void branch_features(const Tree& T, int v, int depth, float qx, float qy, float* f) {
     int4 L = T.lnk[v];
-    float is = 1.0f / T.sq;
+    float is = T.isq;
     float bd[2];
 #pragma unroll
     for (int c = 0; c < 2; ++c) {
@@ -1355,6 +1375,7 @@ __global__ void __launch_bounds__(128) k_prop_dataset(Tree T, const ViewState* v
     if (i >= W || j >= H) return;
     T.n = vs->n;
     T.sq = vs->sq;
+    T.isq = vs->isq;
     int n = T.n;
     if (n < 2) return;
     float qx = (float)i, qy = (float)j;
@@ -1408,6 +1429,7 @@ __global__ void k_prop_init(Tree T, const ViewState* vs, int W, int H, int K, fl
     bool live = i < W && j < H;
     T.n = vs->n;
     T.sq = vs->sq;
+    T.isq = vs->isq;
     size_t pixel = (size_t)j + (size_t)H * i;
     float qx = (float)i, qy = (float)j;
     float m0 = 0.0f;
@@ -1422,7 +1444,7 @@ __global__ void k_prop_init(Tree T, const ViewState* vs, int W, int H, int K, fl
     if (T.n == 1) {  // the root is the only leaf
         for (int k = 0; k < K; ++k) {
             indices[(size_t)K * pixel + k] = T.leaf_id[0];
-            weights[(size_t)K * pixel + k] = hermite_eval(T, 0, T.cen[0], qx, qy) / m0;
+            weights[(size_t)K * pixel + k] = leaf_mass(T, T.cen[0], qx, qy) / m0;
         }
         return;
     }
@@ -1444,6 +1466,7 @@ __global__ void k_prop_features(Tree T, const ViewState* vs, int H, int K, int l
     if (r >= *count) return;
     T.n = vs->n;
     T.sq = vs->sq;
+    T.isq = vs->isq;
     int pixel = draw_in[r] / K;
     float qx = (float)(pixel / H), qy = (float)(pixel % H);
     float f[kFeat];
@@ -1472,6 +1495,7 @@ __global__ void k_prop_step(Tree T, const ViewState* vs, int H, int K, int level
     if (seed_ptr) seed = *seed_ptr;
     T.n = vs->n;
     T.sq = vs->sq;
+    T.isq = vs->isq;
     int draw = draw_in[r];
     int pixel = draw / K, k = draw % K;
     int v = node_in[r];
@@ -1487,7 +1511,7 @@ __global__ void k_prop_step(Tree T, const ViewState* vs, int H, int K, int level
     int c = left ? L.x : L.y;
     if (c >= T.n - 1) {
         float qx = (float)(pixel / H), qy = (float)(pixel % H);
-        float g = hermite_eval(T, c, T.cen[c], qx, qy);
+        float g = leaf_mass(T, T.cen[c], qx, qy);
         indices[draw] = T.leaf_id[c - (T.n - 1)];
         weights[draw] = g / root_mass[pixel] * __expf(-logq);
     } else if (level + 1 < kTrace) {
@@ -1541,6 +1565,7 @@ __global__ void k_fgt_eval(Tree T, const ViewState* vs, int m, const int* __rest
     if (t >= m) return;
     T.n = vs->n;
     T.sq = vs->sq;
+    T.isq = vs->isq;
     out[t] = node_weight(T, nodes[t], q[2 * t], q[2 * t + 1]);
 }
 
@@ -1621,7 +1646,7 @@ static int build_view(const uds_sample_params* p, const Ws& w, int view, const f
 static Tree tree_of(const Ws& w) {
     Tree T;
     T.lnk = w.lnk; T.par = w.par; T.box = w.box; T.cen = w.cen; T.coef = w.coef;
-    T.leaf_xy = w.leaf_xy; T.leaf_id = w.leaf_id; T.n = 0; T.sq = 0.0f;
+    T.leaf_xy = w.leaf_xy; T.leaf_id = w.leaf_id; T.n = 0; T.sq = 0.0f; T.isq = 0.0f;
     return T;
 }
 
