@@ -1093,8 +1093,14 @@ __global__ void __launch_bounds__(128, 3) k_sample(Tree T, const ViewState* vs, 
                 bool mineg = need && v == vv;
                 unsigned grp = __ballot_sync(full, mineg);
                 if (mineg) {
-                    w0 = fmaxf(0.0f, ea >= 0 ? mc.mass[ea] : node_weight(T, a, qx, qy));
-                    w1 = fmaxf(0.0f, eb >= 0 ? mc.mass[eb] : node_weight(T, b, qx, qy));
+                    // one call site: the walk is inlined once, which keeps the
+                    // kernel's hot code small enough for the instruction cache
+#pragma unroll 1
+                    for (int ch = 0; ch < 2; ++ch) {
+                        int en = ch ? eb : ea;
+                        float x = fmaxf(0.0f, en >= 0 ? mc.mass[en] : node_weight(T, ch ? b : a, qx, qy));
+                        if (ch) w1 = x; else w0 = x;
+                    }
                 }
                 pend &= ~grp;
             }
@@ -1265,8 +1271,14 @@ __global__ void __launch_bounds__(128, 3) k_stochastic(Tree T, const ViewState* 
                 bool mineg = need && v == vv;
                 unsigned grp = __ballot_sync(full, mineg);
                 if (mineg) {
-                    w0 = fmaxf(0.0f, ea >= 0 ? mc.mass[ea] : node_weight(T, a, qx, qy));
-                    w1 = fmaxf(0.0f, eb >= 0 ? mc.mass[eb] : node_weight(T, b, qx, qy));
+                    // one call site: the walk is inlined once, which keeps the
+                    // kernel's hot code small enough for the instruction cache
+#pragma unroll 1
+                    for (int ch = 0; ch < 2; ++ch) {
+                        int en = ch ? eb : ea;
+                        float x = fmaxf(0.0f, en >= 0 ? mc.mass[en] : node_weight(T, ch ? b : a, qx, qy));
+                        if (ch) w1 = x; else w0 = x;
+                    }
                 }
                 pend &= ~grp;
             }
