@@ -972,7 +972,7 @@ __device__ void warp_root_walk(const Tree& T, float qx, float qy, bool live, Mas
 }
 
 template <int R, int KM>
-__global__ void __launch_bounds__(128, 3) k_sample(Tree T, const ViewState* vs, int W, int H, int K,
+__global__ void __launch_bounds__(128, 4) k_sample(Tree T, const ViewState* vs, int W, int H, int K,
                                                 float precision, const float* __restrict__ uniforms,
                                                 uint64_t seed, const uint64_t* __restrict__ seed_ptr,
                                                 uint32_t view, int* __restrict__ indices, uds_view_stats* st,
@@ -1199,7 +1199,7 @@ __global__ void __launch_bounds__(128, 3) k_sample(Tree T, const ViewState* vs, 
 // their upper paths, so the child masses of the last path are kept per depth
 // (node ids are unique, so a hit is exact).  A draw that meets two zero
 // masses, or is still above the leaves after kTrace levels, stays -1 / 0.
-__global__ void __launch_bounds__(128, 3) k_stochastic(Tree T, const ViewState* vs, int W, int H, int K,
+__global__ void __launch_bounds__(128, 4) k_stochastic(Tree T, const ViewState* vs, int W, int H, int K,
                                                        float precision, uint64_t seed,
                                                        const uint64_t* __restrict__ seed_ptr, uint32_t view,
                                                        int* __restrict__ indices, float* __restrict__ probs,
