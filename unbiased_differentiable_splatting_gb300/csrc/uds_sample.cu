@@ -809,12 +809,15 @@ __device__ __forceinline__ float hermite_eval(const Tree& T, int v, float4 c, fl
     return w;
 }
 
-__device__ __forceinline__ bool truncated(const Tree& T, int v, float r, float qx, float qy) {
-    float4 b = T.box[v];
+__device__ __forceinline__ bool truncated_box(float4 b, float r, float qx, float qy) {
     float clx = fminf(fmaxf(qx, b.x), b.z), cly = fminf(fmaxf(qy, b.y), b.w);
     float dx = fsub(qx, clx), dy = fsub(qy, cly);
     float d2 = fadd(fadd(0.0f, fmul(dx, dx)), fmul(dy, dy));
     return !(d2 < fmul(r, r));
+}
+
+__device__ __forceinline__ bool truncated(const Tree& T, int v, float r, float qx, float qy) {
+    return truncated_box(T.box[v], r, qx, qy);
 }
 
 // getWeight / accumulateSubtree (evaluateDynamicRadixTree.cuh:129-242):
@@ -875,10 +878,18 @@ struct MassCache {
 // visits exactly that lane's nodes in its own depth-first order, so the
 // running sums are unchanged; but expansion coefficients are now loaded once
 // per warp and the Hermite loops run with warp-uniform bounds.
+//
+// The running sums of a lane's opened ancestors live in shared memory,
+// acc[depth][lane]: every lane inside a node has opened the same ancestors,
+// so the update loop over them has one trip count per warp and touches one
+// bank per lane; each sum is written to the lane's cache once, when its node
+// is closed.
 struct WalkStack {
     int node[kTrace];
     unsigned mask[kTrace];
     int state[kTrace];  // 0 enter, 1 left subtree done, 2 both done
+    int right[kTrace];  // right child of an opened node, kept for state 1
+    float acc[kTrace][32];
 };
 
 __device__ void warp_root_walk(const Tree& T, float qx, float qy, bool live, MassCache& mc, float& total,
@@ -909,13 +920,16 @@ __device__ void warp_root_walk(const Tree& T, float qx, float qy, bool live, Mas
         bool mine = (in >> lane) & 1u;
         __syncwarp();
         if (stt == 0) {
+            // the node's centre, box and links in one round trip to memory
             c = T.cen[v];
+            float4 bx = T.box[v];
+            int4 Lv = T.lnk[v];
             if (meta_degree(c.w) >= 0) {
                 if (mine) {
                     float val = hermite_eval(T, v, c, qx, qy);
                     total = fadd(total, val);
                     if (mc.ok) {
-                        for (int q = 0; q < osp; ++q) mc.mass[ostack[q]] = fadd(mc.mass[ostack[q]], val);
+                        for (int q = 0; q < osp; ++q) ws.acc[q][lane] = fadd(ws.acc[q][lane], val);
                         if (mc.m < kTable) {
                             mc.node[mc.m] = v;
                             mc.mass[mc.m] = val;
@@ -929,7 +943,7 @@ __device__ void warp_root_walk(const Tree& T, float qx, float qy, bool live, Mas
                 --sp;
                 continue;
             }
-            bool op = mine && !truncated(T, v, c.z, qx, qy);
+            bool op = mine && !truncated_box(bx, c.z, qx, qy);
             unsigned opened = __ballot_sync(full, op);
             if (!opened || sp + 1 >= kTrace) {
                 if (opened) mc.ok = false;  // deeper than any tree built here
@@ -939,23 +953,24 @@ __device__ void warp_root_walk(const Tree& T, float qx, float qy, bool live, Mas
             if (op && mc.ok) {
                 if (mc.m < kTable && osp < kTrace) {
                     mc.node[mc.m] = v;
-                    mc.mass[mc.m] = 0.0f;
+                    ws.acc[osp][lane] = 0.0f;
                     ostack[osp++] = mc.m++;
                 } else {
                     mc.ok = false;
                 }
             }
-            int l = T.lnk[v].x;
+            int l = Lv.x;
             if (lane == 0) {
                 ws.mask[sp] = opened;
                 ws.state[sp] = 1;
+                ws.right[sp] = Lv.y;
                 ws.node[sp + 1] = l;
                 ws.mask[sp + 1] = opened;
                 ws.state[sp + 1] = 0;
             }
             ++sp;
         } else if (stt == 1) {
-            int r = T.lnk[v].y;
+            int r = ws.right[sp];
             if (lane == 0) {
                 ws.state[sp] = 2;
                 ws.node[sp + 1] = r;
@@ -964,7 +979,11 @@ __device__ void warp_root_walk(const Tree& T, float qx, float qy, bool live, Mas
             }
             ++sp;
         } else {
-            if (mine && mc.ok) mc.skip[ostack[--osp]] = mc.m;
+            if (mine && mc.ok) {
+                int q = ostack[--osp];
+                mc.mass[q] = ws.acc[osp][lane];
+                mc.skip[q] = mc.m;
+            }
             --sp;
         }
         __syncwarp();
