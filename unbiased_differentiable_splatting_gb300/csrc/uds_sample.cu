@@ -857,15 +857,27 @@ __device__ float node_weight(const Tree& T, int v, float qx, float qy) {
 // expansions below it; one walk from the root therefore yields getWeight of
 // every node it opens if each opened node keeps its own running sum, fed the
 // same values in the same order (so the sums are bit-identical to separate
-// walks).  The opened nodes are stored in pre-order with the index just past
-// their subtree, which locates both children of a cached node; the frontier
-// nodes whose expansion the walk evaluated are stored too.
+// walks).  The opened nodes and the frontier nodes whose expansion the walk
+// evaluated are stored in pre-order, one 8-byte record each: the mass and
+// the entries of the two children.  A child entry is -1 when the child's box
+// misses the truncation circle (it has no expansion, so its getWeight is
+// exactly 0) and -2 below an expansion (not walked: its children's masses
+// are evaluated when needed).  The descent reads one record per child and
+// level.
 constexpr int kTable = 160;
+constexpr int kNotWalked = -2;
+
+__device__ __forceinline__ int2 mass_rec(float mass, int left, int right) {
+    return make_int2(__float_as_int(mass), (int)(((unsigned)left & 0xffffu) | ((unsigned)right << 16)));
+}
+__device__ __forceinline__ float rec_mass(int2 r) { return __int_as_float(r.x); }
+__device__ __forceinline__ int rec_left(int2 r) { return (int)(short)(r.y & 0xffff); }
+__device__ __forceinline__ int rec_right(int2 r) { return r.y >> 16; }
+// the record of a node the cache does not hold
+__device__ __forceinline__ int2 no_record() { return mass_rec(0.0f, kNotWalked, kNotWalked); }
 
 struct MassCache {
-    int node[kTable];
-    float mass[kTable];
-    int skip[kTable];
+    int2 rec[kTable];
     int m;
     bool ok;
 };
@@ -906,7 +918,9 @@ __device__ void warp_root_walk(const Tree& T, float qx, float qy, bool live, Mas
         return;
     }
     if (!liveMask) return;
-    int ostack[kTrace];
+    // per opened ancestor (same index in every lane inside): its entry, its
+    // left child's entry and where its right child's entry would start
+    int ostack[kTrace], lstack[kTrace], rstack[kTrace];
     int osp = 0;
     int sp = 0;
     if (lane == 0) { ws.node[0] = 0; ws.mask[0] = liveMask; ws.state[0] = 0; }
@@ -931,9 +945,7 @@ __device__ void warp_root_walk(const Tree& T, float qx, float qy, bool live, Mas
                     if (mc.ok) {
                         for (int q = 0; q < osp; ++q) ws.acc[q][lane] = fadd(ws.acc[q][lane], val);
                         if (mc.m < kTable) {
-                            mc.node[mc.m] = v;
-                            mc.mass[mc.m] = val;
-                            mc.skip[mc.m] = mc.m + 1;
+                            mc.rec[mc.m] = mass_rec(val, kNotWalked, kNotWalked);
                             ++mc.m;
                         } else {
                             mc.ok = false;
@@ -952,7 +964,6 @@ __device__ void warp_root_walk(const Tree& T, float qx, float qy, bool live, Mas
             }
             if (op && mc.ok) {
                 if (mc.m < kTable && osp < kTrace) {
-                    mc.node[mc.m] = v;
                     ws.acc[osp][lane] = 0.0f;
                     ostack[osp++] = mc.m++;
                 } else {
@@ -970,6 +981,12 @@ __device__ void warp_root_walk(const Tree& T, float qx, float qy, bool live, Mas
             }
             ++sp;
         } else if (stt == 1) {
+            // the left child, if recorded, directly follows its parent
+            if (mine && mc.ok) {
+                int q = ostack[osp - 1];
+                lstack[osp - 1] = mc.m > q + 1 ? q + 1 : -1;
+                rstack[osp - 1] = mc.m;
+            }
             int r = ws.right[sp];
             if (lane == 0) {
                 ws.state[sp] = 2;
@@ -981,8 +998,8 @@ __device__ void warp_root_walk(const Tree& T, float qx, float qy, bool live, Mas
         } else {
             if (mine && mc.ok) {
                 int q = ostack[--osp];
-                mc.mass[q] = ws.acc[osp][lane];
-                mc.skip[q] = mc.m;
+                int rs = rstack[osp];
+                mc.rec[q] = mass_rec(ws.acc[osp][lane], lstack[osp], mc.m > rs ? rs : -1);
             }
             --sp;
         }
@@ -1078,28 +1095,25 @@ __global__ void __launch_bounds__(128, 4) k_sample(Tree T, const ViewState* vs, 
             }
         }
         int v = 0, d = 0;
-        int e = (mc.ok && mc.m > 0) ? 0 : -1;  // cache entry of v
-        unsigned long long cur = 0ull;         // this round's choice bits so far
+        const int2 no_rec = no_record();
+        int2 rc = (mc.ok && mc.m > 0) ? mc.rec[0] : no_rec;  // cache record of v
+        unsigned long long cur = 0ull;                        // this round's choice bits so far
         tp[0] = 1.0f;
         int4 L = T.lnk[0];
         bool going = act && L.w > K;
         while (__any_sync(full, going)) {
             int a = L.x, b = L.y;
             float w0 = 0.0f, w1 = 0.0f;
-            int ea = -1, eb = -1;
+            int2 ra = no_rec, rb = no_rec;  // the children's records
             bool need = false;
             if (going) {
-                if (e >= 0) {
-                    if (e + 1 < mc.m && mc.node[e + 1] == a) ea = e + 1;
-                    int ib = ea >= 0 ? mc.skip[ea] : e + 1;
-                    if (ib < mc.m && mc.node[ib] == b) eb = ib;
-                }
-                if (d < cvn && cv[d] == v) {
+                int ia = rec_left(rc), ib = rec_right(rc);
+                if (ia != kNotWalked) {
+                    if (ia >= 0) { ra = mc.rec[ia]; w0 = fmaxf(0.0f, rec_mass(ra)); }
+                    if (ib >= 0) { rb = mc.rec[ib]; w1 = fmaxf(0.0f, rec_mass(rb)); }
+                } else if (d < cvn && cv[d] == v) {
                     w0 = cw0[d];
                     w1 = cw1[d];
-                } else if (ea >= 0 && eb >= 0) {
-                    w0 = fmaxf(0.0f, mc.mass[ea]);
-                    w1 = fmaxf(0.0f, mc.mass[eb]);
                 } else {
                     need = true;
                 }
@@ -1116,8 +1130,7 @@ __global__ void __launch_bounds__(128, 4) k_sample(Tree T, const ViewState* vs, 
                     // kernel's hot code small enough for the instruction cache
 #pragma unroll 1
                     for (int ch = 0; ch < 2; ++ch) {
-                        int en = ch ? eb : ea;
-                        float x = fmaxf(0.0f, en >= 0 ? mc.mass[en] : node_weight(T, ch ? b : a, qx, qy));
+                        float x = fmaxf(0.0f, node_weight(T, ch ? b : a, qx, qy));
                         if (ch) w1 = x; else w0 = x;
                     }
                 }
@@ -1153,8 +1166,8 @@ __global__ void __launch_bounds__(128, 4) k_sample(Tree T, const ViewState* vs, 
                     going = false;
                     act = false;
                 } else {
-                    if (s0 < s1) { cur |= 1ull << (d - 1); tp[d] = w1; v = b; e = eb; }
-                    else { tp[d] = w0; v = a; e = ea; }
+                    if (s0 < s1) { cur |= 1ull << (d - 1); tp[d] = w1; v = b; rc = rb; }
+                    else { tp[d] = w0; v = a; rc = ra; }
                     L = T.lnk[v];
                     going = L.w > K;
                 }
@@ -1256,7 +1269,8 @@ __global__ void __launch_bounds__(128, 4) k_stochastic(Tree T, const ViewState* 
     bool overflow = false;
     for (int k = 0; k < K; ++k) {
         int v = 0, d = 0;
-        int e = (mc.ok && mc.m > 0) ? 0 : -1;
+        const int2 no_rec = no_record();
+        int2 rc = (mc.ok && mc.m > 0) ? mc.rec[0] : no_rec;
         float prob = 1.0f;
         uint32_t c[4];
         bool ok = act;
@@ -1265,20 +1279,16 @@ __global__ void __launch_bounds__(128, 4) k_stochastic(Tree T, const ViewState* 
         while (__any_sync(full, going)) {
             int a = L.x, b = L.y;
             float w0 = 0.0f, w1 = 0.0f;
-            int ea = -1, eb = -1;
+            int2 ra = no_rec, rb = no_rec;  // the children's records
             bool need = false;
             if (going) {
-                if (e >= 0) {
-                    if (e + 1 < mc.m && mc.node[e + 1] == a) ea = e + 1;
-                    int ib = ea >= 0 ? mc.skip[ea] : e + 1;
-                    if (ib < mc.m && mc.node[ib] == b) eb = ib;
-                }
-                if (d < cvn && cv[d] == v) {
+                int ia = rec_left(rc), ib = rec_right(rc);
+                if (ia != kNotWalked) {
+                    if (ia >= 0) { ra = mc.rec[ia]; w0 = fmaxf(0.0f, rec_mass(ra)); }
+                    if (ib >= 0) { rb = mc.rec[ib]; w1 = fmaxf(0.0f, rec_mass(rb)); }
+                } else if (d < cvn && cv[d] == v) {
                     w0 = cw0[d];
                     w1 = cw1[d];
-                } else if (ea >= 0 && eb >= 0) {
-                    w0 = fmaxf(0.0f, mc.mass[ea]);
-                    w1 = fmaxf(0.0f, mc.mass[eb]);
                 } else {
                     need = true;
                 }
@@ -1294,8 +1304,7 @@ __global__ void __launch_bounds__(128, 4) k_stochastic(Tree T, const ViewState* 
                     // kernel's hot code small enough for the instruction cache
 #pragma unroll 1
                     for (int ch = 0; ch < 2; ++ch) {
-                        int en = ch ? eb : ea;
-                        float x = fmaxf(0.0f, en >= 0 ? mc.mass[en] : node_weight(T, ch ? b : a, qx, qy));
+                        float x = fmaxf(0.0f, node_weight(T, ch ? b : a, qx, qy));
                         if (ch) w1 = x; else w0 = x;
                     }
                 }
@@ -1318,8 +1327,8 @@ __global__ void __launch_bounds__(128, 4) k_stochastic(Tree T, const ViewState* 
                     going = false;
                 } else {
                     float r0 = fdiv(w0, sum);
-                    if (u <= r0) { prob = fmul(prob, r0); v = a; e = ea; }
-                    else { prob = fmul(prob, fdiv(w1, sum)); v = b; e = eb; }
+                    if (u <= r0) { prob = fmul(prob, r0); v = a; rc = ra; }
+                    else { prob = fmul(prob, fdiv(w1, sum)); v = b; rc = rb; }
                     ++d;
                     if (d >= kTrace && v < n - 1) {
                         ok = false;
