@@ -1071,29 +1071,8 @@ __global__ void __launch_bounds__(128, 4) k_sample(Tree T, const ViewState* vs, 
     int cv[kTrace];
     float cw0[kTrace], cw1[kTrace];
     int cvn = 0;
-    float u[KM];
     bool overflow = false;
     for (int r = 0; r < R; ++r) {
-        if (act) {
-            if (uniforms) {
-                const float* up = uniforms + ((size_t)pixel * R + r) * K;
-#pragma unroll UK
-                for (int k = 0; k < KM; ++k)
-                    if (k < K) u[k] = up[k];
-            } else {
-                int G = (K + 3) >> 2;
-#pragma unroll UK
-                for (int g = 0; g < (KM + 3) / 4; ++g) {
-                    if (g < G) {
-                        uint32_t c4[4] = {(uint32_t)pixel, view, (uint32_t)(r * G + g), 0u};
-                        philox4x32_10(c4, (uint32_t)seed, (uint32_t)(seed >> 32));
-#pragma unroll
-                        for (int q = 0; q < 4; ++q)
-                            if (4 * g + q < KM) u[4 * g + q] = bits_to_uniform(c4[q]);
-                    }
-                }
-            }
-        }
         int v = 0, d = 0;
         const int2 no_rec = no_record();
         int2 rc = (mc.ok && mc.m > 0) ? mc.rec[0] : no_rec;  // cache record of v
@@ -1192,12 +1171,23 @@ __global__ void __launch_bounds__(128, 4) k_sample(Tree T, const ViewState* vs, 
         // sequentialPoissonRadixTree.cuh:15-41); a leaf's mass is its own
         // Gaussian (degree 0, coefficient 1)
         int f0 = L.z, cnt = L.w;
+        // the round's uniforms, drawn as the leaves use them (after the
+        // descent, so they hold no registers there): Philox block
+        // (pixel, view, r * ceil(K / 4) + k / 4), or the caller's tensor
+        const float* up = uniforms ? uniforms + ((size_t)pixel * R + r) * K : nullptr;
+        const int G = (K + 3) >> 2;
+        uint32_t c4[4];
 #pragma unroll UK
         for (int k = 0; k < KM; ++k) {
             if (k < cnt) {
+                if (!up && (k & 3) == 0) {
+                    c4[0] = (uint32_t)pixel; c4[1] = view; c4[2] = (uint32_t)(r * G + (k >> 2)); c4[3] = 0u;
+                    philox4x32_10(c4, (uint32_t)seed, (uint32_t)(seed >> 32));
+                }
+                float uk = up ? up[k] : bits_to_uniform(c4[k & 3]);
                 int leafNode = T.n - 1 + f0 + k;
                 float pw = fmaxf(0.0f, leaf_mass(T, T.cen[leafNode], qx, qy));
-                float key = fdiv(u[k], pw);
+                float key = fdiv(uk, pw);
                 int index = T.leaf_id[f0 + k];
                 bool done = false;
 #pragma unroll UK
@@ -1280,8 +1270,11 @@ __global__ void __launch_bounds__(128, 4) k_stochastic(Tree T, const ViewState* 
             int a = L.x, b = L.y;
             float w0 = 0.0f, w1 = 0.0f;
             int2 ra = no_rec, rb = no_rec;  // the children's records
+            int4 La = L, Lb = L;            // and links, loaded with them
             bool need = false;
             if (going) {
+                La = T.lnk[a];
+                Lb = T.lnk[b];
                 int ia = rec_left(rc), ib = rec_right(rc);
                 if (ia != kNotWalked) {
                     if (ia >= 0) { ra = mc.rec[ia]; w0 = fmaxf(0.0f, rec_mass(ra)); }
@@ -1327,15 +1320,14 @@ __global__ void __launch_bounds__(128, 4) k_stochastic(Tree T, const ViewState* 
                     going = false;
                 } else {
                     float r0 = fdiv(w0, sum);
-                    if (u <= r0) { prob = fmul(prob, r0); v = a; rc = ra; }
-                    else { prob = fmul(prob, fdiv(w1, sum)); v = b; rc = rb; }
+                    if (u <= r0) { prob = fmul(prob, r0); v = a; rc = ra; L = La; }
+                    else { prob = fmul(prob, fdiv(w1, sum)); v = b; rc = rb; L = Lb; }
                     ++d;
                     if (d >= kTrace && v < n - 1) {
                         ok = false;
                         overflow = true;
                         going = false;
                     } else {
-                        L = T.lnk[v];
                         going = v < n - 1;
                     }
                 }
