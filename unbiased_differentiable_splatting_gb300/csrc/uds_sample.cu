@@ -883,13 +883,18 @@ struct MassCache {
 };
 
 // Warp-cooperative walk.  The 32 pixels of a warp (an 8 x 4 tile) walk the
-// union of their trees in lock-step with an explicit stack of (node, lanes
-// inside, state) in shared memory.  At a node, every lane inside tests its
+// union of their trees in lock-step.  At a node, every lane inside tests its
 // own truncation circle; lanes that open the node continue into its children,
 // the others leave that subtree.  Restricted to one lane, the union walk
 // visits exactly that lane's nodes in its own depth-first order, so the
 // running sums are unchanged; but expansion coefficients are now loaded once
 // per warp and the Hermite loops run with warp-uniform bounds.
+//
+// Each iteration enters one node (its centre, box and links in one round
+// trip to memory); the stack in shared memory holds the opened ancestors
+// (lanes that opened each, its right child), and whether an ancestor's right
+// subtree is under way is one bit of a register.  After a node that is not
+// descended into, finished ancestors are closed in the same iteration.
 //
 // The running sums of a lane's opened ancestors live in shared memory,
 // acc[depth][lane]: every lane inside a node has opened the same ancestors,
@@ -897,10 +902,8 @@ struct MassCache {
 // bank per lane; each sum is written to the lane's cache once, when its node
 // is closed.
 struct WalkStack {
-    int node[kTrace];
-    unsigned mask[kTrace];
-    int state[kTrace];  // 0 enter, 1 left subtree done, 2 both done
-    int right[kTrace];  // right child of an opened node, kept for state 1
+    unsigned mask[kTrace];  // lanes that opened the ancestor at this depth
+    int right[kTrace];      // its right child
     float acc[kTrace][32];
 };
 
@@ -922,88 +925,88 @@ __device__ void warp_root_walk(const Tree& T, float qx, float qy, bool live, Mas
     // left child's entry and where its right child's entry would start
     int ostack[kTrace], lstack[kTrace], rstack[kTrace];
     int osp = 0;
-    int sp = 0;
-    if (lane == 0) { ws.node[0] = 0; ws.mask[0] = liveMask; ws.state[0] = 0; }
-    __syncwarp();
-    int budget = 6 * T.n + 64;
-    while (sp >= 0) {
+    int sp = -1;                    // deepest opened ancestor of v
+    unsigned long long onright = 0; // bit k: ancestor k's right subtree is under way
+    int v = 0;                      // node entered next, and the lanes inside it
+    unsigned in = liveMask;
+    int budget = 4 * T.n + 64;
+    while (true) {
         if (--budget < 0) { mc.ok = false; break; }
-        int v = ws.node[sp];
-        unsigned in = ws.mask[sp];
-        int stt = ws.state[sp];
         bool mine = (in >> lane) & 1u;
-        __syncwarp();
-        if (stt == 0) {
-            // the node's centre, box and links in one round trip to memory
-            c = T.cen[v];
-            float4 bx = T.box[v];
-            int4 Lv = T.lnk[v];
-            if (meta_degree(c.w) >= 0) {
-                if (mine) {
-                    float val = hermite_eval(T, v, c, qx, qy);
-                    total = fadd(total, val);
-                    if (mc.ok) {
-                        for (int q = 0; q < osp; ++q) ws.acc[q][lane] = fadd(ws.acc[q][lane], val);
-                        if (mc.m < kTable) {
-                            mc.rec[mc.m] = mass_rec(val, kNotWalked, kNotWalked);
-                            ++mc.m;
-                        } else {
-                            mc.ok = false;
-                        }
+        c = T.cen[v];
+        float4 bx = T.box[v];
+        int4 Lv = T.lnk[v];
+        bool descend = false;
+        if (meta_degree(c.w) >= 0) {
+            if (mine) {
+                float val = hermite_eval(T, v, c, qx, qy);
+                total = fadd(total, val);
+                if (mc.ok) {
+                    for (int q = 0; q < osp; ++q) ws.acc[q][lane] = fadd(ws.acc[q][lane], val);
+                    if (mc.m < kTable) {
+                        mc.rec[mc.m] = mass_rec(val, kNotWalked, kNotWalked);
+                        ++mc.m;
+                    } else {
+                        mc.ok = false;
                     }
                 }
-                --sp;
-                continue;
             }
+        } else {
             bool op = mine && !truncated_box(bx, c.z, qx, qy);
             unsigned opened = __ballot_sync(full, op);
-            if (!opened || sp + 1 >= kTrace) {
-                if (opened) mc.ok = false;  // deeper than any tree built here
-                --sp;
-                continue;
-            }
-            if (op && mc.ok) {
-                if (mc.m < kTable && osp < kTrace) {
-                    ws.acc[osp][lane] = 0.0f;
-                    ostack[osp++] = mc.m++;
-                } else {
-                    mc.ok = false;
+            // v sits at depth sp + 1; its children would be at sp + 2
+            if (opened && sp + 2 >= kTrace) {
+                mc.ok = false;  // deeper than any tree built here
+            } else if (opened) {
+                if (op && mc.ok) {
+                    if (mc.m < kTable && osp < kTrace) {
+                        ws.acc[osp][lane] = 0.0f;
+                        ostack[osp++] = mc.m++;
+                    } else {
+                        mc.ok = false;
+                    }
                 }
+                ++sp;
+                onright &= ~(1ull << sp);
+                if (lane == 0) {
+                    ws.mask[sp] = opened;
+                    ws.right[sp] = Lv.y;
+                }
+                v = Lv.x;
+                in = opened;
+                descend = true;
             }
-            int l = Lv.x;
-            if (lane == 0) {
-                ws.mask[sp] = opened;
-                ws.state[sp] = 1;
-                ws.right[sp] = Lv.y;
-                ws.node[sp + 1] = l;
-                ws.mask[sp + 1] = opened;
-                ws.state[sp + 1] = 0;
+        }
+        __syncwarp();
+        if (descend) continue;
+        // climb: close ancestors whose right subtree is done; at the first
+        // one whose left subtree is done, continue with its right child
+        bool more = false;
+        while (sp >= 0) {
+            unsigned pin = ws.mask[sp];
+            bool pm = (pin >> lane) & 1u;
+            if (!((onright >> sp) & 1ull)) {
+                // the left child, if recorded, directly follows its parent
+                if (pm && mc.ok) {
+                    int q = ostack[osp - 1];
+                    lstack[osp - 1] = mc.m > q + 1 ? q + 1 : -1;
+                    rstack[osp - 1] = mc.m;
+                }
+                onright |= 1ull << sp;
+                v = ws.right[sp];
+                in = pin;
+                more = true;
+                break;
             }
-            ++sp;
-        } else if (stt == 1) {
-            // the left child, if recorded, directly follows its parent
-            if (mine && mc.ok) {
-                int q = ostack[osp - 1];
-                lstack[osp - 1] = mc.m > q + 1 ? q + 1 : -1;
-                rstack[osp - 1] = mc.m;
-            }
-            int r = ws.right[sp];
-            if (lane == 0) {
-                ws.state[sp] = 2;
-                ws.node[sp + 1] = r;
-                ws.mask[sp + 1] = in;
-                ws.state[sp + 1] = 0;
-            }
-            ++sp;
-        } else {
-            if (mine && mc.ok) {
+            if (pm && mc.ok) {
                 int q = ostack[--osp];
                 int rs = rstack[osp];
                 mc.rec[q] = mass_rec(ws.acc[osp][lane], lstack[osp], mc.m > rs ? rs : -1);
             }
             --sp;
         }
-        __syncwarp();
+        if (!more) break;
+        __syncwarp();  // the stack slots read above may be rewritten next
     }
 }
 
