@@ -698,9 +698,16 @@ __global__ void __launch_bounds__(32 * kP2MWarps) k_p2m(const ViewState* vs, con
             for (int j = 0; j < cnt; ++j) {
                 float yb = ty[j * kTStride + b];
                 const float* row = tx + j * kTStride + g;
+                // rows in blocks of four behind a check of the lane's row
+                // count, so a low degree issues only the rows it has
 #pragma unroll
-                for (int r = 0; r <= kMaxDegree; ++r)
-                    if (r < nrows) acc[r] = __fmaf_rn(row[r * G], yb, acc[r]);
+                for (int r0 = 0; r0 <= kMaxDegree; r0 += 4) {
+                    if (r0 < nrows) {
+#pragma unroll
+                        for (int r = r0; r < r0 + 4 && r <= kMaxDegree; ++r)
+                            if (r < nrows) acc[r] = __fmaf_rn(row[r * G], yb, acc[r]);
+                    }
+                }
             }
         }
         __syncwarp();
