@@ -45,6 +45,17 @@ __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a,
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
 
+// One double operation on float operands, rounded to float, is the float
+// operation itself: rounding to 53 bits and then to 24 is innocuous for +, -,
+// *, / and sqrt because 53 >= 2 * 24 + 2 (S. A. Figueroa, "When is double
+// rounding innocuous?", SIGNUM Newsletter 30(3), 1995); overflow and
+// subnormal results round the same way too.  So the reference's
+// (float)(1.0 / (double)x) or (float)((double)x + 1.0) runs here as a float
+// operation with the identical result, off the slow FP64 pipe.
+__device__ __forceinline__ float div_via_double(float a, float b) { return fdiv(a, b); }
+__device__ __forceinline__ float add_via_double(float a, float b) { return fadd(a, b); }
+__device__ __forceinline__ float sub_via_double(float a, float b) { return fsub(a, b); }
+
 // --------------------------------------------- deterministic exp and log
 // exp: Cody & Waite (1980) reduction x = k ln2 + r with ln2 split in a high
 // and a low part, degree-7 Taylor polynomial of e^r in Horner form with

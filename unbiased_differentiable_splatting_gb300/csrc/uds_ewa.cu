@@ -131,8 +131,8 @@ __global__ void k_ewa_chain(int B, int N, float W, float H, float f, const float
     // forward quantities (same sequence as the frame)
     float sp[2];
     screen_point(W, H, f, p, sp);
-    float y0[2] = {(float)dadd((double)sp[0], 1.0), sp[1]};
-    float y1[2] = {sp[0], (float)dadd((double)sp[1], 1.0)};
+    float y0[2] = {add_via_double(sp[0], 1.0f), sp[1]};
+    float y1[2] = {sp[0], add_via_double(sp[1], 1.0f)};
     float x0[3], x1[3], t0[3], t1[3];
     back_project(W, H, f, y0, x0);
     back_project(W, H, f, y1, x1);
@@ -142,7 +142,7 @@ __global__ void k_ewa_chain(int B, int N, float W, float H, float f, const float
     tangent(x0, p, n, t0);
     tangent(x1, p, n, t1);
     float al = fsqrt(dot3(t0, t0));
-    float invNorm = (float)ddiv(1.0, (double)al);
+    float invNorm = div_via_double(1.0f, al);
     float u0[3] = {t0[0] * invNorm, t0[1] * invNorm, t0[2] * invNorm};
     float u1[3];
     cross3(u0, n, u1);

@@ -10,10 +10,10 @@ __device__ __forceinline__ float dot3(const float* a, const float* b) {
     return fadd(fadd(fadd(0.0f, fmul(a[0], b[0])), fmul(a[1], b[1])), fmul(a[2], b[2]));
 }
 
-// toScreenspace: -(x f)/z + W/2.0 (the addend is double)
+// toScreenspace: -(x f)/z + W/2.0 (the addend is double; W/2 is a float)
 __device__ __forceinline__ void screen_point(float W, float H, float f, const float* p, float* s) {
-    s[0] = (float)dadd((double)fdiv(-fmul(p[0], f), p[2]), (double)W / 2.0);
-    s[1] = (float)dadd((double)fdiv(fmul(p[1], f), p[2]), (double)H / 2.0);
+    s[0] = add_via_double(fdiv(-fmul(p[0], f), p[2]), fmul(W, 0.5f));
+    s[1] = add_via_double(fdiv(fmul(p[1], f), p[2]), fmul(H, 0.5f));
 }
 
 // backproject (double arithmetic, rounded to float)
@@ -40,15 +40,15 @@ struct EwaFrame {
 __device__ __forceinline__ void ewa_frame(float W, float H, float f, const float* p, const float* n,
                                           const float* sd, float sm, EwaFrame& F) {
     screen_point(W, H, f, p, F.sp);
-    float y0[2] = {(float)dadd((double)F.sp[0], 1.0), F.sp[1]};
-    float y1[2] = {F.sp[0], (float)dadd((double)F.sp[1], 1.0)};
+    float y0[2] = {add_via_double(F.sp[0], 1.0f), F.sp[1]};
+    float y1[2] = {F.sp[0], add_via_double(F.sp[1], 1.0f)};
     float x0[3], x1[3], t0[3], t1[3];
     back_project(W, H, f, y0, x0);
     back_project(W, H, f, y1, x1);
     tangent(x0, p, n, t0);
     tangent(x1, p, n, t1);
     float nt0 = fsqrt(dot3(t0, t0));
-    float invNorm = (float)ddiv(1.0, (double)nt0);
+    float invNorm = div_via_double(1.0f, nt0);
     float u0[3] = {fmul(t0[0], invNorm), fmul(t0[1], invNorm), fmul(t0[2], invNorm)};
     float u1[3] = {fsub(fmul(u0[1], n[2]), fmul(u0[2], n[1])), fsub(fmul(u0[2], n[0]), fmul(u0[0], n[2])),
                    fsub(fmul(u0[0], n[1]), fmul(u0[1], n[0]))};
@@ -58,7 +58,7 @@ __device__ __forceinline__ void ewa_frame(float W, float H, float f, const float
     F.invJ[3] = dot3(t1, u1);
     const float* iJ = F.invJ;
     float det = fsub(fmul(iJ[0], iJ[3]), fmul(iJ[1], iJ[2]));
-    float invDet = (float)ddiv(1.0, (double)det);
+    float invDet = div_via_double(1.0f, det);
     float J[4] = {fmul(iJ[3], invDet), fmul(-iJ[1], invDet), fmul(-iJ[2], invDet), fmul(iJ[0], invDet)};
     float D[4] = {fmul(sd[0], sd[0]), 0.0f, 0.0f, fmul(sd[1], sd[1])};
     float T[4], U[4];
@@ -86,7 +86,7 @@ __device__ __forceinline__ void ewa_frame(float W, float H, float f, const float
 __device__ __forceinline__ void ewa_gauss_consts(const EwaFrame& F, float4& a, float4& b) {
     const float* V = F.V;
     float vdet = fsub(fmul(V[0], V[3]), fmul(V[1], V[2]));
-    float inv = (float)ddiv(1.0, (double)vdet);
+    float inv = div_via_double(1.0f, vdet);
     float jdet = fsub(fmul(F.invJ[0], F.invJ[3]), fmul(F.invJ[1], F.invJ[2]));
     float norm = (float)dmul(dmul(2.0 * kPi, (double)fsqrt(vdet)), (double)fabsf(jdet));
     a = make_float4(F.sp[0], F.sp[1], fmul(V[3], inv), fmul(-V[1], inv));

@@ -15,7 +15,7 @@ constexpr int kFilterThreads = 64;
 __device__ __forceinline__ void pixel_ray(float W, float H, float f, float px, float py, float* dir) {
     float s[2] = {px, py}, wd[3];
     back_project(W, H, f, s, wd);
-    float inv = (float)ddiv(1.0, (double)fsqrt(dot3(wd, wd)));
+    float inv = div_via_double(1.0f, fsqrt(dot3(wd, wd)));
 #pragma unroll
     for (int i = 0; i < 3; ++i) dir[i] = fmul(fmul(wd[i], inv), -1.0f);
 }

@@ -121,15 +121,27 @@ __device__ __forceinline__ float splat_bandwidth(float W, float H, float f, cons
     ewa_frame(W, H, f, p, n, sd, sm, F);
     const float* V = F.V;
     float det = fsub(fmul(V[0], V[3]), fmul(V[1], V[2]));
-    float inv = (float)ddiv(1.0, (double)det);
+    float inv = div_via_double(1.0f, det);
     float i0 = fmul(V[3], inv), i1 = fmul(-V[1], inv), i2 = fmul(-V[2], inv), i3 = fmul(V[0], inv);
     float tr = fadd(i0, i3);
-    float idet = fsub(fmul(i0, i3), fmul(i1, i2));
-    float root = fsqrt((float)dsub(dmul(0.25, (double)fmul(tr, tr)), (double)idet));
-    float l1 = (float)dadd(dmul(0.5, (double)tr), (double)root);
-    float l2 = (float)dsub(dmul(0.5, (double)tr), (double)root);
+    float tt = fmul(tr, tr);
+    float root, l1, l2;
+    if (fabsf(tr) >= 0x1p-100f && fabsf(tt) >= 0x1p-100f) {
+        // 0.25 tt and 0.5 tr are exact in float as in double, so each
+        // double operation below has float operands
+        root = fsqrt(sub_via_double(fmul(0.25f, tt), fsub(fmul(i0, i3), fmul(i1, i2))));
+        l1 = add_via_double(fmul(0.5f, tr), root);
+        l2 = sub_via_double(fmul(0.5f, tr), root);
+    } else {  // tiny (or NaN) trace: the reference's double sequence
+        float idet = fsub(fmul(i0, i3), fmul(i1, i2));
+        root = fsqrt((float)dsub(dmul(0.25, (double)tt), (double)idet));
+        l1 = (float)dadd(dmul(0.5, (double)tr), (double)root);
+        l2 = (float)dsub(dmul(0.5, (double)tr), (double)root);
+    }
     float lk = fminf(l1, l2);
-    return (float)fmin(1.0, ddiv(1.0, (double)fsqrt(lk)));
+    // (float)fmin(1.0, 1.0 / (double)sqrt(lk)): the min commutes with the
+    // monotone rounding, and fminf returns 1 for a NaN quotient as fmin does
+    return fminf(1.0f, div_via_double(1.0f, fsqrt(lk)));
 }
 
 __global__ void k_bandwidth(int N, float W, float H, float f, const float* __restrict__ pts,
@@ -143,7 +155,7 @@ __global__ void k_bandwidth(int N, float W, float H, float f, const float* __res
         float d[2] = {sd[2 * (size_t)x], sd[2 * (size_t)x + 1]};
         float hk = splat_bandwidth(W, H, f, p, n, d, sm);
         if (isfinite(hk)) {
-            s = (unsigned long long)__double2ll_rn(dmul((double)hk, 4294967296.0));
+            s = (unsigned long long)__float2ll_rn(fmul(hk, 4294967296.0f));  // exact: hk <= 1
             c = 1;
         }
     }

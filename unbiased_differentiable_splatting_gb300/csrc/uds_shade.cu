@@ -117,7 +117,7 @@ __device__ __forceinline__ float sh_unit(const float* n, float* v) {
     float norm = fsqrt(fadd(fadd(fadd(0.0f, fmul(n[0], n[0])), fmul(n[1], n[1])), fmul(n[2], n[2])));
     v[0] = 0.0f; v[1] = 0.0f; v[2] = 0.0f; v[3] = 1.0f;
     if (norm > 1e-5f) {
-        float inv = (float)ddiv(1.0, (double)norm);
+        float inv = div_via_double(1.0f, norm);
         v[0] = fmul(n[0], inv); v[1] = fmul(n[1], inv); v[2] = fmul(n[2], inv); v[3] = fmul(norm, inv);
     }
     return norm;
