@@ -3,6 +3,7 @@
 // ewaSplatting.cuh:8-91, linalg.cuh), and its reverse-mode derivative.
 #pragma once
 #include "uds_common.cuh"
+#include "uds_backproject.cuh"
 
 namespace uds {
 
@@ -16,11 +17,14 @@ __device__ __forceinline__ void screen_point(float W, float H, float f, const fl
     s[1] = add_via_double(fdiv(fmul(p[1], f), p[2]), fmul(H, 0.5f));
 }
 
-// backproject (double arithmetic, rounded to float)
+// backproject (double arithmetic, rounded to float): the same numbers from
+// the exact integer quotient where it applies, else the double sequence
 __device__ __forceinline__ void back_project(float W, float H, float f, const float* s, float* x) {
-    double f2 = dmul(2.0, (double)f);
-    x[0] = (float)ddiv(dsub((double)W, dmul(2.0, (double)s[0])), f2);
-    x[1] = (float)ddiv(-dsub((double)H, dmul(2.0, (double)s[1])), f2);
+    float q;
+    if (bp_quotient(fmul(W, 0.5f), s[0], f, &q)) x[0] = q;
+    else x[0] = (float)ddiv(dsub((double)W, dmul(2.0, (double)s[0])), dmul(2.0, (double)f));
+    if (bp_quotient(fmul(H, 0.5f), s[1], f, &q)) x[1] = -q;
+    else x[1] = (float)ddiv(-dsub((double)H, dmul(2.0, (double)s[1])), dmul(2.0, (double)f));
     x[2] = 1.0f;
 }
 
