@@ -652,16 +652,38 @@ __global__ void k_assign(ViewState* vs, float4* cen, const uint32_t* __restrict_
 // its leaves in Morton order: C_ab = sum_i t_a(s0_i) t_b(s1_i) with
 // t_a(s) = s^a / a!, s = (leaf - centre) * (1 / sqrt(2 h^2)).  One warp per
 // internal node.  For a chunk of 32 leaves each lane builds one leaf's
-// t-tables in shared memory (t_a = (t_{a-1} s) * (1 / a)); lane (g, b) then owns
-// column b and rows a = g, g + G, ... (G = 32 / (p+1) row groups) and adds
-// fma(t_a(s0), t_b(s1), C_ab) leaf by leaf, so every coefficient is summed in
-// leaf order exactly as the oracle's deterministic flavour does.
+// t-tables in shared memory (t_a = (t_{a-1} s) * (1 / a)); each lane then
+// owns a block of BR rows x BC columns of C (the block shape depends on the
+// degree, so that the blocks of a (p+1)^2 table fit 32 lanes) and adds
+// fma(t_a(s0), t_b(s1), C_ab) leaf by leaf: every coefficient is summed in
+// leaf order exactly as the oracle's deterministic flavour does, and one
+// shared-memory read feeds BR or BC multiply-adds.
 constexpr int kP2MWarps = 4;
 // 1 / a, rounded once at compile time (the oracle uses the same constants)
 __constant__ float kInvInt[kMaxDegree + 1] = {0.0f, 1.0f / 1, 1.0f / 2, 1.0f / 3, 1.0f / 4, 1.0f / 5, 1.0f / 6,
                                               1.0f / 7, 1.0f / 8, 1.0f / 9, 1.0f / 10, 1.0f / 11, 1.0f / 12,
                                               1.0f / 13, 1.0f / 14, 1.0f / 15, 1.0f / 16};
 constexpr int kTStride = kMaxDegree + 1;  // odd: conflict-free row writes
+// rows x columns per lane for p + 1 = 1 .. 17 coefficients per side
+__constant__ unsigned char kP2MBlock[kMaxDegree + 2][2] = {
+    {1, 1}, {1, 1}, {1, 1}, {1, 1}, {1, 1}, {1, 1}, {1, 2}, {1, 2}, {1, 2},
+    {1, 3}, {2, 2}, {2, 3}, {2, 3}, {2, 4}, {2, 4}, {2, 4}, {2, 4}, {3, 4}};
+
+template <int BR, int BC>
+__device__ __forceinline__ void p2m_block(const float* tx, const float* ty, int cnt, const int* ra, const int* cb,
+                                          float (&acc)[3][4]) {
+    for (int j = 0; j < cnt; ++j) {
+        float xv[BR], yv[BC];
+#pragma unroll
+        for (int i = 0; i < BR; ++i) xv[i] = tx[j * kTStride + ra[i]];
+#pragma unroll
+        for (int k = 0; k < BC; ++k) yv[k] = ty[j * kTStride + cb[k]];
+#pragma unroll
+        for (int i = 0; i < BR; ++i)
+#pragma unroll
+            for (int k = 0; k < BC; ++k) acc[i][k] = __fmaf_rn(xv[i], yv[k], acc[i][k]);
+    }
+}
 
 __global__ void __launch_bounds__(32 * kP2MWarps) k_p2m(const ViewState* vs, const int4* __restrict__ lnk,
                                                         const float4* __restrict__ cen,
@@ -679,13 +701,22 @@ __global__ void __launch_bounds__(32 * kP2MWarps) k_p2m(const ViewState* vs, con
     int4 L = lnk[v];
     float isq = vs->isq;
     int P1 = p + 1;
-    int G = 32 / P1;
-    int b = lane % P1, g = lane / P1;
-    bool owner = g < G;
-    int nrows = owner ? (P1 - g + G - 1) / G : 0;
-    float acc[kMaxDegree + 1];
+    int BR = kP2MBlock[P1][0], BC = kP2MBlock[P1][1];
+    int nC = (P1 + BC - 1) / BC, nR = (P1 + BR - 1) / BR;
+    int gr = lane / nC, gc = lane % nC;
+    bool owner = gr < nR;
+    // this lane's rows and columns; reads past the table repeat its last
+    // row / column (their sums are not written)
+    int ra[3], cb[4];
 #pragma unroll
-    for (int r = 0; r <= kMaxDegree; ++r) acc[r] = 0.0f;
+    for (int i = 0; i < 3; ++i) ra[i] = min(gr * BR + i, p);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) cb[k] = min(gc * BC + k, p);
+    float acc[3][4];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) acc[i][k] = 0.0f;
     float* tx = s_tx[warp];
     float* ty = s_ty[warp];
     int end = L.z + L.w;
@@ -707,26 +738,27 @@ __global__ void __launch_bounds__(32 * kP2MWarps) k_p2m(const ViewState* vs, con
         }
         __syncwarp();
         if (owner) {
-            for (int j = 0; j < cnt; ++j) {
-                float yb = ty[j * kTStride + b];
-                const float* row = tx + j * kTStride + g;
-                // rows in blocks of four behind a check of the lane's row
-                // count, so a low degree issues only the rows it has
-#pragma unroll
-                for (int r0 = 0; r0 <= kMaxDegree; r0 += 4) {
-                    if (r0 < nrows) {
-#pragma unroll
-                        for (int r = r0; r < r0 + 4 && r <= kMaxDegree; ++r)
-                            if (r < nrows) acc[r] = __fmaf_rn(row[r * G], yb, acc[r]);
-                    }
-                }
+            switch (BR * 8 + BC) {  // uniform over the warp
+                case 9: p2m_block<1, 1>(tx, ty, cnt, ra, cb, acc); break;
+                case 10: p2m_block<1, 2>(tx, ty, cnt, ra, cb, acc); break;
+                case 11: p2m_block<1, 3>(tx, ty, cnt, ra, cb, acc); break;
+                case 18: p2m_block<2, 2>(tx, ty, cnt, ra, cb, acc); break;
+                case 19: p2m_block<2, 3>(tx, ty, cnt, ra, cb, acc); break;
+                case 20: p2m_block<2, 4>(tx, ty, cnt, ra, cb, acc); break;
+                default: p2m_block<3, 4>(tx, ty, cnt, ra, cb, acc); break;
             }
         }
         __syncwarp();
     }
+    if (owner) {
 #pragma unroll
-    for (int r = 0; r <= kMaxDegree; ++r)
-        if (r < nrows) coef[off + (g + r * G) * P1 + b] = acc[r];
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                int a = gr * BR + i, b = gc * BC + k;
+                if (i < BR && k < BC && a <= p && b <= p) coef[off + a * P1 + b] = acc[i][k];
+            }
+    }
 }
 
 // -------------------------------------------------------- FGT evaluation
