@@ -1,7 +1,9 @@
 // Compares the integer back-projection quotient (uds_backproject.cuh) with
 // the double formula it replaces, bit for bit, on random and edge-case
-// inputs.  Built and run by test_backproject.py (g++ -ffp-contract=off).
-// Prints "<cases> <fast-path cases> <mismatches>".
+// inputs, and checks the single-operation rule the kernels' *_via_double
+// helpers rely on ((float)(a op b in double) == a op b in float for
+// + - * /).  Built and run by test_backproject.py (g++ -ffp-contract=off).
+// Prints "<quotient cases> <integer-path cases> <single-op cases> <mismatches>".
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -27,7 +29,7 @@ int main(int argc, char** argv) {
     long n = argc > 1 ? std::atol(argv[1]) : 2000000;
     std::mt19937_64 rng(12345);
     std::uniform_real_distribution<double> U(0.0, 1.0);
-    long cases = 0, fast = 0, bad = 0;
+    long cases = 0, fast = 0, ops = 0, bad = 0;
     auto check = [&](float W, float s, float f) {
         ++cases;
         float got;
@@ -74,6 +76,29 @@ int main(int argc, char** argv) {
         for (int si = -128; si <= 256; ++si)
             for (float f : {1.0f, 3.0f, 7.0f, 100.0f, 525.0f, 1111.1f})
                 check((float)Wi, (float)si * 0.25f, f);
-    std::printf("%ld %ld %ld\n", cases, fast, bad);
+    // the single-operation rule behind div_via_double / add_via_double /
+    // sub_via_double: (float)(a op b in double) == a op b in float
+    auto rnd_float = [&]() {
+        uint32_t b = (uint32_t)rng();
+        float x;
+        std::memcpy(&x, &b, 4);
+        return x;
+    };
+    for (long i = 0; i < n; ++i) {
+        float a = rnd_float(), b = (i & 1) ? rnd_float() : (float)(U(rng) * 2.0 - 0.5);
+        if (i % 3 == 0) a = 1.0f;  // the reference's 1.0 / x and x + 1.0
+        if (!std::isfinite(a) || !std::isfinite(b)) continue;
+        volatile double da = a, db = b;
+        float pairs[4][2] = {{(float)(da / db), a / b}, {(float)(da + db), a + b},
+                             {(float)(da - db), a - b}, {(float)(da * db), a * b}};
+        for (auto& p : pairs) {
+            ++ops;
+            if (!(std::isnan(p[0]) && std::isnan(p[1])) && bits(p[0]) != bits(p[1])) {
+                if (bad < 10) std::printf("single-op mismatch a=%a b=%a\n", a, b);
+                ++bad;
+            }
+        }
+    }
+    std::printf("%ld %ld %ld %ld\n", cases, fast, ops, bad);
     return bad != 0;
 }
