@@ -301,6 +301,21 @@ int uds_shade_sh_backward(int B, int P, const float* grad, const float* coeffs, 
                           const float* normals, const float* diffuse, float* grad_coeffs,
                           float* grad_normals, float* grad_diffuse, void* stream);
 
+/* ---- Lambert of the forward shading mode, fused (shading.py:12-29
+ *      Lambert.forward: ambient * diffuse + sum_l I_l clamp(<dir_l, n>, 0, 1)
+ *      diffuse / pi, a chain of broadcasting tensor operations in the
+ *      reference).  normals (B, N, 3), diffuse (dB, N, 3), dirs (B, L, 3),
+ *      intensities (IB, L, 3), ambient (aB, 3); dB, IB, aB in {1, B};
+ *      L <= 4.  The backward sums the gradients of broadcast operands. ---- */
+int uds_lambert_forward(int B, int N, int L, const float* ambient, int aB, const float* dirs,
+                        const float* intensities, int IB, const float* normals,
+                        const float* diffuse, int dB, float* out, void* stream);
+int uds_lambert_backward(int B, int N, int L, const float* grad, const float* ambient, int aB,
+                         const float* dirs, const float* intensities, int IB, const float* normals,
+                         const float* diffuse, int dB, float* grad_ambient, float* grad_dirs,
+                         float* grad_intensities, float* grad_normals, float* grad_diffuse,
+                         void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -224,6 +224,136 @@ __global__ void k_shade_sh_backward(int B, int P, const float* __restrict__ gin,
     }
 }
 
+// Per-splat Lambert of the forward shading mode (shading.py:12-29, a chain
+// of broadcasting tensor operations in the reference), fused:
+//   out = ambient * d + sum_l (I_l * clamp(<dir_l, n>, 0, 1)) * (d / pi)
+// with normals (B, N, 3), diffuse d (dB, N, 3), dirs (B, L, 3), intensities
+// (IB, L, 3), ambient (aB, 3); dB, IB, aB are 1 or B.  Each product and sum
+// is rounded as the tensor operations round it (the division by pi is a
+// multiplication by the float reciprocal, as PyTorch divides by a scalar).
+constexpr int kLambertMaxL = 4;
+constexpr float kInvPiF = (float)(1.0 / kPi);
+
+__global__ void k_lambert_forward(int B, int N, int L, const float* __restrict__ amb, int aB,
+                                  const float* __restrict__ dirs, const float* __restrict__ I, int IB,
+                                  const float* __restrict__ nrm, const float* __restrict__ dif, int dB,
+                                  float* __restrict__ out) {
+    size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (size_t)N * B) return;
+    int b = (int)(t / N);
+    size_t n = t - (size_t)b * N;
+    const float* nv = nrm + 3 * t;
+    const float* d = dif + 3 * ((dB > 1 ? (size_t)b * N : 0) + n);
+    const float* a = amb + 3 * (aB > 1 ? b : 0);
+    float S[3] = {0.0f, 0.0f, 0.0f};
+    for (int l = 0; l < L; ++l) {
+        const float* dl = dirs + 3 * ((size_t)b * L + l);
+        const float* il = I + 3 * ((IB > 1 ? (size_t)b * L : 0) + l);
+        float c = fadd(fadd(fmul(dl[0], nv[0]), fmul(dl[1], nv[1])), fmul(dl[2], nv[2]));
+        c = fminf(fmaxf(c, 0.0f), 1.0f);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            float tk = fmul(fmul(il[k], c), fmul(d[k], kInvPiF));
+            S[k] = l ? fadd(S[k], tk) : tk;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) out[3 * t + k] = fadd(fmul(a[k], d[k]), S[k]);
+}
+
+// One thread per splat, looping over the views: the normal gradients per
+// (view, splat), the diffuse gradient summed over the views in registers
+// when diffuse is shared, and the light / ambient gradients reduced over the
+// warp, then the block (shared memory), then one atomic per block and value.
+__global__ void k_lambert_backward(int B, int N, int L, const float* __restrict__ g,
+                                   const float* __restrict__ amb, int aB, const float* __restrict__ dirs,
+                                   const float* __restrict__ I, int IB, const float* __restrict__ nrm,
+                                   const float* __restrict__ dif, int dB, float* __restrict__ gamb,
+                                   float* __restrict__ gdirs, float* __restrict__ gI, float* __restrict__ gn,
+                                   float* __restrict__ gd) {
+    extern __shared__ float red[];  // gdirs (B L 3), gI (IB L 3), gamb (aB 3)
+    float* rD = red;
+    float* rI = rD + 3 * B * L;
+    float* rA = rI + 3 * IB * L;
+    int nred = 3 * B * L + 3 * IB * L + 3 * aB;
+    for (int i = threadIdx.x; i < nred; i += blockDim.x) red[i] = 0.0f;
+    __syncthreads();
+    size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool live = n < (size_t)N;
+    int lane = threadIdx.x & 31;
+    float gds[3] = {0.0f, 0.0f, 0.0f};  // diffuse gradient summed over the views (dB == 1)
+    for (int b = 0; b < B; ++b) {
+        float gv[3] = {0, 0, 0}, nv[3] = {0, 0, 0}, d[3] = {0, 0, 0};
+        const float* a = amb + 3 * (aB > 1 ? b : 0);
+        if (live) {
+            size_t t = (size_t)b * N + n;
+            const float* dp = dif + 3 * ((dB > 1 ? (size_t)b * N : 0) + n);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) { gv[k] = g[3 * t + k]; nv[k] = nrm[3 * t + k]; d[k] = dp[k]; }
+        }
+        float gnv[3] = {0.0f, 0.0f, 0.0f}, gdv[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) gdv[k] = fmul(gv[k], a[k]);
+        // ambient: g * d
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            float v = fmul(gv[k], d[k]);
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) atomicAdd(&rA[3 * (aB > 1 ? b : 0) + k], v);
+        }
+        for (int l = 0; l < L; ++l) {
+            const float* dl = dirs + 3 * ((size_t)b * L + l);
+            const float* il = I + 3 * ((IB > 1 ? (size_t)b * L : 0) + l);
+            float s = fadd(fadd(fmul(dl[0], nv[0]), fmul(dl[1], nv[1])), fmul(dl[2], nv[2]));
+            float c = fminf(fmaxf(s, 0.0f), 1.0f);
+            bool pass = s >= 0.0f && s <= 1.0f;  // clamp passes the gradient inside [0, 1]
+            float gs = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                float brdf = fmul(d[k], kInvPiF);
+                gs += gv[k] * il[k] * brdf;
+                gdv[k] += gv[k] * il[k] * c * kInvPiF;
+                float vI = gv[k] * c * brdf;
+                for (int o = 16; o > 0; o >>= 1) vI += __shfl_xor_sync(0xffffffffu, vI, o);
+                if (lane == 0) atomicAdd(&rI[3 * ((IB > 1 ? b : 0) * L + l) + k], vI);
+            }
+            if (!pass) gs = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                gnv[k] += gs * dl[k];
+                float vD = gs * nv[k];
+                for (int o = 16; o > 0; o >>= 1) vD += __shfl_xor_sync(0xffffffffu, vD, o);
+                if (lane == 0) atomicAdd(&rD[3 * (b * L + l) + k], vD);
+            }
+        }
+        if (live) {
+            size_t t = (size_t)b * N + n;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) gn[3 * t + k] = gnv[k];
+            if (dB > 1) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) gd[3 * t + k] = gdv[k];
+            } else {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) gds[k] += gdv[k];
+            }
+        }
+    }
+    if (live && dB == 1) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) gd[3 * n + k] = gds[k];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nred; i += blockDim.x) {
+        float v = red[i];
+        if (v != 0.0f) {
+            if (i < 3 * B * L) atomicAdd(&gdirs[i], v);
+            else if (i < 3 * B * L + 3 * IB * L) atomicAdd(&gI[i - 3 * B * L], v);
+            else atomicAdd(&gamb[i - 3 * B * L - 3 * IB * L], v);
+        }
+    }
+}
+
 }  // namespace uds
 
 using namespace uds;
@@ -275,5 +405,46 @@ extern "C" int uds_shade_sh_backward(int B, int P, const float* grad, const floa
     if (P == 0) return UDS_OK;
     k_shade_sh_backward<<<cdiv((size_t)P * B, kShadeThreads), kShadeThreads, 0, s>>>(
         B, P, grad, coeffs, cB, normals, diffuse, grad_coeffs, grad_normals, grad_diffuse);
+    return launch_status();
+}
+
+static size_t lambert_shared(int B, int L, int IB, int aB) {
+    return sizeof(float) * (3 * (size_t)B * L + 3 * (size_t)IB * L + 3 * (size_t)aB);
+}
+
+extern "C" int uds_lambert_forward(int B, int N, int L, const float* ambient, int aB, const float* dirs,
+                                   const float* intensities, int IB, const float* normals,
+                                   const float* diffuse, int dB, float* out, void* stream) {
+    if (B <= 0 || N < 0 || L < 0 || L > kLambertMaxL || (aB != 1 && aB != B) || (IB != 1 && IB != B) ||
+        (dB != 1 && dB != B) || !ambient || (L > 0 && (!dirs || !intensities)))
+        return UDS_ERR_ARGUMENT;
+    if (N == 0) return UDS_OK;
+    if (!normals || !diffuse || !out) return UDS_ERR_ARGUMENT;
+    k_lambert_forward<<<cdiv((size_t)N * B, kShadeThreads), kShadeThreads, 0, as_stream(stream)>>>(
+        B, N, L, ambient, aB, dirs, intensities, IB, normals, diffuse, dB, out);
+    return launch_status();
+}
+
+extern "C" int uds_lambert_backward(int B, int N, int L, const float* grad, const float* ambient, int aB,
+                                    const float* dirs, const float* intensities, int IB, const float* normals,
+                                    const float* diffuse, int dB, float* grad_ambient, float* grad_dirs,
+                                    float* grad_intensities, float* grad_normals, float* grad_diffuse,
+                                    void* stream) {
+    if (B <= 0 || N < 0 || L < 0 || L > kLambertMaxL || (aB != 1 && aB != B) || (IB != 1 && IB != B) ||
+        (dB != 1 && dB != B) || !ambient || !grad_ambient || (L > 0 && (!dirs || !intensities || !grad_dirs ||
+                                                                        !grad_intensities)))
+        return UDS_ERR_ARGUMENT;
+    size_t shm = lambert_shared(B, L, IB, aB);
+    if (shm > 48 * 1024) return UDS_ERR_ARGUMENT;
+    cudaStream_t s = as_stream(stream);
+    cudaError_t e = cudaMemsetAsync(grad_ambient, 0, sizeof(float) * 3 * (size_t)aB, s);
+    if (e == cudaSuccess && L > 0) e = cudaMemsetAsync(grad_dirs, 0, sizeof(float) * 3 * (size_t)B * L, s);
+    if (e == cudaSuccess && L > 0) e = cudaMemsetAsync(grad_intensities, 0, sizeof(float) * 3 * (size_t)IB * L, s);
+    if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
+    if (N == 0) return UDS_OK;
+    if (!grad || !normals || !diffuse || !grad_normals || !grad_diffuse) return UDS_ERR_ARGUMENT;
+    k_lambert_backward<<<cdiv((size_t)N, kShadeThreads), kShadeThreads, shm, s>>>(
+        B, N, L, grad, ambient, aB, dirs, intensities, IB, normals, diffuse, dB, grad_ambient, grad_dirs,
+        grad_intensities, grad_normals, grad_diffuse);
     return launch_status();
 }

@@ -171,6 +171,21 @@ class DiffuseShading(th.autograd.Function):
         return tuple(shading.backward(gradIn.contiguous(), directions, intensites, normals, diffuse))
 
 
+class LambertShading(th.autograd.Function):
+    """Per-splat Lambert of the forward shading mode (shading.py:12-29),
+    fused into one kernel each way."""
+
+    @staticmethod
+    def forward(ctx, ambient, directions, intensities, normals, diffuse):
+        ts = [t.contiguous() for t in (ambient, directions, intensities, normals, diffuse)]
+        ctx.save_for_backward(*ts)
+        return shading.lambertForward(*ts)
+
+    @staticmethod
+    def backward(ctx, gradIn):
+        return tuple(shading.lambertBackward(gradIn.contiguous(), *ctx.saved_tensors))
+
+
 class SphericalHarmonicShading(th.autograd.Function):
     @staticmethod
     def forward(ctx, coefficients, normals, diffuse):
@@ -185,7 +200,8 @@ class SphericalHarmonicShading(th.autograd.Function):
 
 
 __all__ = ["FmmSampling", "AffineTransform", "LinearTransform", "EWASplatting", "DepthFiltering",
-           "LinearInterpolation", "DiffuseShading", "SphericalHarmonicShading", "world2Camera", "transformForward",
+           "LinearInterpolation", "DiffuseShading", "LambertShading", "SphericalHarmonicShading", "world2Camera",
+           "transformForward",
            "conditionalNormalization", "normalize", "dot"]
 
 

@@ -18,9 +18,10 @@ from dataclasses import dataclass
 
 import torch as th
 
+from .cudaExtensions import shading as _shading
 from .extensions import (AffineTransform, DepthFiltering, DiffuseShading, EWASplatting, FmmSampling,
-                         LinearInterpolation, LinearTransform, SphericalHarmonicShading, dot, normalize,
-                         transformForward, world2Camera)
+                         LambertShading, LinearInterpolation, LinearTransform, SphericalHarmonicShading, dot,
+                         normalize, transformForward, world2Camera)
 
 
 @dataclass
@@ -40,17 +41,24 @@ def _cosine(normal: th.Tensor, light: th.Tensor) -> th.Tensor:
 
 
 class BackfaceCulling(th.nn.Module):
-    """render.py:193-205: flip normals that face away from the camera."""
+    """render.py:193-205: flip normals that face away from the camera.  With
+    ``normals`` None only the camera-space normals are flipped (the shading
+    modes that do not read the flipped world normals)."""
 
     def forward(self, normals, camNormals):
         facing = camNormals[..., 2].unsqueeze(-1) > 0
-        return th.where(facing, -normals, normals), th.where(facing, -camNormals, camNormals)
+        flipped = None if normals is None else th.where(facing, -normals, normals)
+        return flipped, th.where(facing, -camNormals, camNormals)
 
 
 class Lambert(th.nn.Module):
-    """shading.py:12-29: per-splat ambient + Lambert shading."""
+    """shading.py:12-29: per-splat ambient + Lambert shading: one fused kernel
+    each way when the operands have the shapes it takes (the renderer's),
+    else the reference's tensor expression."""
 
     def forward(self, ambientLight, lampDirections, lampIntensities, normals, diffuse):
+        if _shading.lambert_shapes(ambientLight, lampDirections, lampIntensities, normals, diffuse) is not None:
+            return LambertShading.apply(ambientLight, lampDirections, lampIntensities, normals, diffuse)
         bn, l, _ = lampDirections.shape
         lampDirections = lampDirections.view(bn, l, 1, 3)
         normals = normals.unsqueeze(1)
@@ -150,7 +158,10 @@ class Splatting(th.nn.Module):
         transformMatrix = transformForward(transformMatrix, self.coordForward).squeeze(1).contiguous()
         camPoints = self.affineTransform(transformMatrix, pointPositions)
         camNormals = self.linearTransform(transformMatrix, pointNormals)
-        pointNormals, backfaceNormals = self.backface(pointNormals, camNormals)
+        harmonics = self.shadingMode in ("sphericalHarmonics", "forwardHarmonics")
+        flipped, backfaceNormals = self.backface(pointNormals if harmonics else None, camNormals)
+        if harmonics:
+            pointNormals = flipped
         with th.no_grad():
             indices = self.sampling(self.width, self.height, self.focallength, camPoints.detach(),
                                     backfaceNormals.detach().contiguous(), pointDiffuse, pointStdDevs.detach(),
