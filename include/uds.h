@@ -90,6 +90,15 @@ int uds_transform_forward(int affine, int B, const float* M, int vB, int N, cons
 int uds_transform_backward(int affine, int B, const float* grad, const float* M, int vB, int N,
                            const float* v, float* gM, float* gv, void* stream);
 
+/* ---- world2Camera (utils.py:11-49, tensor operations in the reference):
+ *      positions (B, 3) and quaternions (B, 4) as (x, y, z, w) to row-major
+ *      view matrices (B, 4, 4) = [R | t; 0 0 0 1], bit-identical to the
+ *      reference's operation sequence; the backward maps d/dM to d/dt, d/dq. ---- */
+int uds_view_matrix_forward(int B, const float* positions, const float* quaternions, float* matrices,
+                            void* stream);
+int uds_view_matrix_backward(int B, const float* grad, const float* quaternions, float* grad_positions,
+                             float* grad_quaternions, void* stream);
+
 /* ---- sampling.sample (sampling.cpp:48-94): points, normals (B,N,3)
  *      camera space, stdDevs (std_batch,N,2) -> indices (B,W,H,K) int32,
  *      -1 where no sample.  uniforms: optional (B,W,H,R,K) float32 in (0,1],

@@ -41,6 +41,8 @@ _SIGS = {
     "uds_transform_forward": (c_int, [c_int, c_int, c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p]),
     "uds_transform_backward": (c_int, [c_int, c_int, c_void_p, c_void_p, c_int, c_int, c_void_p, c_void_p,
                                        c_void_p, c_void_p]),
+    "uds_view_matrix_forward": (c_int, [c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "uds_view_matrix_backward": (c_int, [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "uds_sample_workspace_size": (c_size_t, [ctypes.POINTER(SampleParams)]),
     "uds_sample": (c_int, [ctypes.POINTER(SampleParams), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                            c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),

@@ -87,6 +87,63 @@ __global__ void k_transform_backward(int B, const float* __restrict__ grad,
     }
 }
 
+// world2Camera (utils.py:11-49): quaternion (x, y, z, w) and position to the
+// view matrix [R | t; 0 0 0 1], R by the Euler-Rodrigues formula, with every
+// product and sum rounded as the reference's tensor operations round them
+// (left to right), so the matrix is the same bit for bit.  One thread per
+// view; the backward is the analytic derivative of R in the quaternion.
+__global__ void k_view_matrix_forward(int B, const float* __restrict__ pos, const float* __restrict__ quat,
+                                      float* __restrict__ M) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    float x = quat[4 * b], y = quat[4 * b + 1], z = quat[4 * b + 2], w = quat[4 * b + 3];
+    float x2 = fmul(x, x), y2 = fmul(y, y), z2 = fmul(z, z), w2 = fmul(w, w);
+    float xy = fmul(x, y), zw = fmul(z, w), xz = fmul(x, z), yw = fmul(y, w), yz = fmul(y, z), xw = fmul(x, w);
+    float* m = M + 16 * (size_t)b;
+    m[0] = fadd(fsub(fsub(x2, y2), z2), w2);
+    m[1] = fmul(2.0f, fsub(xy, zw));
+    m[2] = fmul(2.0f, fadd(xz, yw));
+    m[3] = pos[3 * b];
+    m[4] = fmul(2.0f, fadd(xy, zw));
+    m[5] = fadd(fsub(fadd(-x2, y2), z2), w2);
+    m[6] = fmul(2.0f, fsub(yz, xw));
+    m[7] = pos[3 * b + 1];
+    m[8] = fmul(2.0f, fsub(xz, yw));
+    m[9] = fmul(2.0f, fadd(yz, xw));
+    m[10] = fadd(fadd(fsub(-x2, y2), z2), w2);
+    m[11] = pos[3 * b + 2];
+    m[12] = 0.0f;
+    m[13] = 0.0f;
+    m[14] = 0.0f;
+    m[15] = 1.0f;
+}
+
+__global__ void k_view_matrix_backward(int B, const float* __restrict__ G, const float* __restrict__ quat,
+                                       float* __restrict__ gpos, float* __restrict__ gquat) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    float x = quat[4 * b], y = quat[4 * b + 1], z = quat[4 * b + 2], w = quat[4 * b + 3];
+    const float* g = G + 16 * (size_t)b;
+    gpos[3 * b] = g[3];
+    gpos[3 * b + 1] = g[7];
+    gpos[3 * b + 2] = g[11];
+    // dR_ij / d(x, y, z, w), row-major i, j
+    const float d[9][4] = {{2 * x, -2 * y, -2 * z, 2 * w}, {2 * y, 2 * x, -2 * w, -2 * z},
+                           {2 * z, 2 * w, 2 * x, 2 * y},   {2 * y, 2 * x, 2 * w, 2 * z},
+                           {-2 * x, 2 * y, -2 * z, 2 * w}, {-2 * w, 2 * z, 2 * y, -2 * x},
+                           {2 * z, -2 * w, 2 * x, -2 * y}, {2 * w, 2 * z, 2 * y, 2 * x},
+                           {-2 * x, -2 * y, 2 * z, 2 * w}};
+    float gq[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+    for (int e = 0; e < 9; ++e) {
+        float ge = g[4 * (e / 3) + e % 3];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) gq[k] += ge * d[e][k];
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) gquat[4 * b + k] = gq[k];
+}
+
 }  // namespace uds
 
 using namespace uds;
@@ -112,5 +169,22 @@ extern "C" int uds_transform_backward(int affine, int B, const float* grad, cons
     dim3 grid(cdiv(N, 256), B);
     if (affine) k_transform_backward<true><<<grid, 256, 0, s>>>(B, grad, M, vB, N, v, gM, gv);
     else k_transform_backward<false><<<grid, 256, 0, s>>>(B, grad, M, vB, N, v, gM, gv);
+    return launch_status();
+}
+
+extern "C" int uds_view_matrix_forward(int B, const float* positions, const float* quaternions, float* matrices,
+                                       void* stream) {
+    if (B < 0 || (B > 0 && (!positions || !quaternions || !matrices))) return UDS_ERR_ARGUMENT;
+    if (B == 0) return UDS_OK;
+    k_view_matrix_forward<<<cdiv((size_t)B, 128), 128, 0, as_stream(stream)>>>(B, positions, quaternions, matrices);
+    return launch_status();
+}
+
+extern "C" int uds_view_matrix_backward(int B, const float* grad, const float* quaternions, float* grad_positions,
+                                        float* grad_quaternions, void* stream) {
+    if (B < 0 || (B > 0 && (!grad || !quaternions || !grad_positions || !grad_quaternions))) return UDS_ERR_ARGUMENT;
+    if (B == 0) return UDS_OK;
+    k_view_matrix_backward<<<cdiv((size_t)B, 128), 128, 0, as_stream(stream)>>>(B, grad, quaternions,
+                                                                                  grad_positions, grad_quaternions);
     return launch_status();
 }

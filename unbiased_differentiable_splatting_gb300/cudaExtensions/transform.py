@@ -1,4 +1,5 @@
-"""cudaExtensions.transform (transform.cpp:33-86)."""
+"""cudaExtensions.transform (transform.cpp:33-86), and the view matrix of
+world2Camera (utils.py:11-49)."""
 from __future__ import annotations
 
 import torch
@@ -47,3 +48,25 @@ def linearForward(transformation, vector):
 
 def linearBackward(gradIn, transformation, vector):
     return _backward(False, gradIn, transformation, vector)
+
+
+def viewMatrixForward(positions: torch.Tensor, quaternions: torch.Tensor) -> torch.Tensor:
+    """(B, 3) positions, (B, 4) quaternions (x, y, z, w) -> (B, 1, 4, 4)."""
+    need(positions, "positions")
+    need(quaternions, "quaternions", device=positions.device)
+    B = quaternions.shape[0]
+    out = torch.empty((B, 1, 4, 4), dtype=torch.float32, device=positions.device)
+    check(load().uds_view_matrix_forward(B, ptr(positions), ptr(quaternions), ptr(out), stream_ptr(positions.device)),
+          "view matrix forward")
+    return out
+
+
+def viewMatrixBackward(gradIn: torch.Tensor, quaternions: torch.Tensor):
+    need(gradIn, "gradIn")
+    need(quaternions, "quaternions", device=gradIn.device)
+    B = quaternions.shape[0]
+    gp = torch.empty((B, 3), dtype=torch.float32, device=gradIn.device)
+    gq = torch.empty_like(quaternions)
+    check(load().uds_view_matrix_backward(B, ptr(gradIn), ptr(quaternions), ptr(gp), ptr(gq),
+                                          stream_ptr(gradIn.device)), "view matrix backward")
+    return gp, gq

@@ -27,10 +27,34 @@ def dot(x: th.Tensor, y: th.Tensor, keepdim: bool) -> th.Tensor:
     return th.sum(x.mul(y), dim=-1, keepdim=keepdim)
 
 
+class ViewMatrix(th.autograd.Function):
+    """world2Camera on the GPU: one kernel each way (the forward rounds like
+    the reference's tensor operations, so the matrix is the same)."""
+
+    @staticmethod
+    def forward(ctx, camPositions, camQuaternion):
+        q = camQuaternion.contiguous()
+        ctx.save_for_backward(q)
+        ctx.pshape = camPositions.shape
+        return transform.viewMatrixForward(camPositions.reshape(-1, 3).contiguous(), q)
+
+    @staticmethod
+    def backward(ctx, gradIn):
+        (q,) = ctx.saved_tensors
+        gp, gq = transform.viewMatrixBackward(gradIn.contiguous(), q)
+        return gp.reshape(ctx.pshape), gq
+
+
 def world2Camera(camPositions: th.Tensor, camQuaternion: th.Tensor) -> th.Tensor:
     """Quaternion (x, y, z, w) + translation -> (B,1,4,4) view matrix
-    (Euler-Rodrigues rotation, utils.py:11-49); differentiable in torch."""
+    (Euler-Rodrigues rotation, utils.py:11-49): the fused kernels for float32
+    CUDA tensors of shapes (B,3) and (B,4), else the tensor expression."""
     B = camPositions.shape[0]
+    if (camPositions.is_cuda and camQuaternion.is_cuda and camPositions.dtype == th.float32
+            and camQuaternion.dtype == th.float32 and camPositions.device == camQuaternion.device
+            and camQuaternion.dim() == 2 and camQuaternion.shape[1] == 4 and camPositions.numel() == 3 * B
+            and camQuaternion.shape[0] == B):
+        return ViewMatrix.apply(camPositions, camQuaternion)
     x, y, z, w = camQuaternion.split(1, dim=-1)
     x2, y2, z2, w2 = x * x, y * y, z * z, w * w
     xy, zw, xz, yw, yz, xw = x * y, z * w, x * z, y * w, y * z, x * w
