@@ -441,6 +441,94 @@ def proposal_main(args):
     }), flush=True)
 
 
+def next_rows_main(args):
+    """The rows either side of the path, on the 500k / 1024^2 / K=8 view's
+    own sample lists: pixel scatter and gather (atomic and deterministic),
+    the nearest-sample lists, the fused image loss and the splat Adam step.
+    Device-resident inputs, L2 flushed (256 MiB write) before each timed
+    call, CUDA events on the launching stream, median of --steps calls;
+    achieved GB/s = algorithmic bytes / time, against the measured HBM copy
+    bandwidth."""
+    import torch
+    from unbiased_differentiable_splatting_gb300 import load, training
+    from unbiased_differentiable_splatting_gb300.extensions import transformForward, world2Camera
+    from unbiased_differentiable_splatting_gb300.cudaExtensions import (nearestsamples, pixelgather, sampling,
+                                                                        splatting, transform)
+    if args.impl == "reference":
+        print(json.dumps({"impl": "reference", "unavailable": "the next-row kernels are timed for this build only; "
+                          "the reference arm times the default workload"}))
+        return
+    load()
+    dev = torch.device("cuda", 0)
+    wl = WORKLOADS["harmonic500k"]
+    sc = make_scene(wl)
+    W = H = wl["width"]
+    K, f = wl["K"], sc["focal"]
+    d = {k: v.to(dev) for k, v in sc.items() if isinstance(v, torch.Tensor)}
+    with torch.no_grad():
+        M = transformForward(world2Camera(d["cam_positions"], d["cam_orientations"]), "-z").squeeze(1).contiguous()
+        cp = transform.affineForward(M, d["points"])
+        cn = transform.linearForward(M, d["normals"])
+        cnb = torch.where(cn[..., 2:] > 0, -cn, cn).contiguous()
+        idx = sampling.sample(W, H, f, cp, cnb, d["colors"], d["stddevs"], K, 0.0, wl["precision"], seed=1)
+        wts = splatting.forward(W, H, f, idx, cp, cn, d["stddevs"], 0.0)
+    N, C, S = cp.shape[1], 3, W * H * K
+    valid = int((idx >= 0).sum())
+    g = torch.Generator(device=dev).manual_seed(0)
+    vals_splat = torch.rand((1, N, C), generator=g, device=dev)
+    vals_sample = torch.rand((1, W, H, K, C), generator=g, device=dev)
+    img = torch.rand((1, W, H, C), generator=g, device=dev)
+    tgt = torch.rand((1, W, H, C), generator=g, device=dev)
+    params = [torch.rand((1, N, c), generator=g, device=dev) for c in (3, 3, C, 2)]
+    for t in params:
+        t.grad = torch.rand(t.shape, generator=g, device=dev)
+    opt = training.SplatAdam(*params)
+    loss = training.L2ImageLoss("sum")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak = json.load(open(peaks_path))["hbm_gbs"] if os.path.exists(peaks_path) else 6800.0
+
+    def timed(fn):
+        for _ in range(max(args.warmup, 3)):
+            fn()
+        ts = []
+        for _ in range(max(args.steps, 1)):
+            flush.fill_(1)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.median(ts))
+
+    rows = {}
+
+    def row(name, fn, nbytes, what):
+        ms = timed(fn)
+        gbs = nbytes / (ms * 1e-3) / 1e9
+        rows[name] = {"ms": ms, "bytes_alg": int(nbytes), "GB/s": gbs, "frac_of_hbm": gbs / peak, "what": what}
+
+    with torch.no_grad():
+        row("pixel_scatter", lambda: pixelgather.scatter(idx, vals_splat), 4 * S + 4 * C * S + 4 * C * valid,
+            "indices read, C values per valid sample gathered, C per sample written")
+        row("pixel_gather_atomic", lambda: pixelgather.gather(idx, vals_sample, N, False),
+            4 * S + 4 * C * S + 4 * C * N, "indices and C values per sample read, C per splat written")
+        row("pixel_gather_deterministic", lambda: pixelgather.gather(idx, vals_sample, N, True),
+            4 * S + 4 * C * S + 4 * C * N, "as the atomic gather; the per-splat ordering is extra traffic")
+        row("nearest_samples", lambda: nearestsamples.nearest(idx, wts, cp, 8), 8 * S + N * (12 + 4 * 8),
+            "indices and weights per sample, points and 8 neighbours per splat")
+        row("image_loss_l2", lambda: loss(img, tgt), 3 * 4 * W * H * C, "image and target read, gradient written")
+        row("splat_adam", opt.step, N * (3 + 3 + C + 2) * 28,
+            "per value: parameter read and written, gradient read, two moments read and written")
+    print(json.dumps({"metric": "next-row kernels, ms per call", "workload": "harmonic500k: 500000 surfels, "
+                      "1024x1024, K=8 sample lists", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                      "samples": S, "valid_samples": valid, "splats": N, "peak_hbm_gbs": peak,
+                      "l2": "flushed (256 MiB write) before each call", "rows": rows}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -448,7 +536,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="harmonic500k",
-                    choices=sorted(WORKLOADS) + sorted(MULTIVIEW) + ["proposal"])
+                    choices=sorted(WORKLOADS) + sorted(MULTIVIEW) + ["proposal", "next"])
     ap.add_argument("--seeds", type=int, default=8, help="proposal workload: sampling calls per method")
     ap.add_argument("--train-steps", type=int, default=600, help="proposal workload: Adam steps")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
@@ -456,6 +544,8 @@ def main():
     args = ap.parse_args()
     if args.workload == "proposal":
         return proposal_main(args)
+    if args.workload == "next":
+        return next_rows_main(args)
     if args.workload in MULTIVIEW:
         return multiview_main(args, args.workload, MULTIVIEW[args.workload])
     wl = WORKLOADS[args.workload]
