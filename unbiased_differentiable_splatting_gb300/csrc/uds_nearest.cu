@@ -16,6 +16,7 @@
 // bucket.  Distances use exact-rounding operations, so the order matches the
 // oracle's bit for bit.
 #include "uds_common.cuh"
+#include "uds_scan.cuh"
 
 namespace uds {
 
@@ -55,28 +56,6 @@ __global__ void k_nearest_pairs(size_t P, int K, int N, const int* __restrict__ 
     }
 }
 
-__global__ void k_nearest_scan(size_t M, const unsigned* __restrict__ count, unsigned* __restrict__ offs) {
-    __shared__ unsigned part[1024];
-    size_t per = (M + blockDim.x - 1) / blockDim.x;
-    size_t lo = threadIdx.x * per, hi = min(M, lo + per);
-    unsigned s = 0;
-    for (size_t i = lo; i < hi; ++i) s += count[i];
-    part[threadIdx.x] = s;
-    __syncthreads();
-    for (int o = 1; o < (int)blockDim.x; o <<= 1) {
-        unsigned v = threadIdx.x >= (unsigned)o ? part[threadIdx.x - o] : 0;
-        __syncthreads();
-        part[threadIdx.x] += v;
-        __syncthreads();
-    }
-    unsigned run = threadIdx.x > 0 ? part[threadIdx.x - 1] : 0;
-    for (size_t i = lo; i < hi; ++i) {
-        offs[i] = run;
-        run += count[i];
-    }
-    if (threadIdx.x == blockDim.x - 1) offs[M] = part[threadIdx.x];
-}
-
 constexpr int kMaxNearest = 32;
 
 __global__ void k_nearest_select(int N, int M, const float* __restrict__ pts, const unsigned* __restrict__ offs,
@@ -114,7 +93,7 @@ extern "C" size_t uds_nearest_workspace_size(int B, int W, int H, int K, int N) 
     if (B <= 0 || W <= 0 || H <= 0 || K <= 0 || N < 0) return 0;
     auto a = [](size_t x) { return (x + 255) & ~(size_t)255; };
     size_t S = (size_t)B * W * H * K;
-    return 2 * a(4 * (size_t)N) + a(4 * ((size_t)N + 1)) + a(4 * S);
+    return 2 * a(4 * (size_t)N) + a(4 * ((size_t)N + 1)) + a(4 * S) + a(4 * scan_part_entries((size_t)N));
 }
 
 extern "C" int uds_nearest_samples(int B, int W, int H, int K, const int32_t* indices, const float* weights, int N,
@@ -132,14 +111,16 @@ extern "C" int uds_nearest_samples(int B, int W, int H, int K, const int32_t* in
     unsigned* fill = reinterpret_cast<unsigned*>(p + a(4 * (size_t)N));
     unsigned* offs = reinterpret_cast<unsigned*>(p + 2 * a(4 * (size_t)N));
     int* cand = reinterpret_cast<int*>(p + 2 * a(4 * (size_t)N) + a(4 * ((size_t)N + 1)));
+    unsigned* part = reinterpret_cast<unsigned*>(p + 2 * a(4 * (size_t)N) + a(4 * ((size_t)N + 1)) +
+                                                 a(4 * (size_t)B * W * H * K));
     cudaError_t e = cudaMemsetAsync(count, 0, 2 * a(4 * (size_t)N), s);
     if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
     size_t P = (size_t)B * W * H;
     // all views' pixels feed one list per splat (points (1, N, 3), as the
     // reference assumes)
     k_nearest_pairs<<<cdiv(P, 256), 256, 0, s>>>(P, K, N, indices, weights, count, nullptr, nullptr, nullptr, 0);
-    k_nearest_scan<<<1, 1024, 0, s>>>((size_t)N, count, offs);
+    exclusive_scan((size_t)N, count, offs, part, s);
     k_nearest_pairs<<<cdiv(P, 256), 256, 0, s>>>(P, K, N, indices, weights, nullptr, offs, fill, cand, 1);
     k_nearest_select<<<cdiv(N, 128), 128, 0, s>>>(N, num_nearest, points, offs, cand, nearest);
-    return launch_status(4);
+    return launch_status(6);
 }

@@ -14,6 +14,7 @@
 //     its splat's values in that order, so the result is bit-identical to a
 //     sequential sum in sample order.
 #include "uds_common.cuh"
+#include "uds_scan.cuh"
 
 namespace uds {
 
@@ -64,30 +65,6 @@ __global__ void k_pixel_count(size_t S, size_t per_view, int N, const int* __res
     if (t >= S) return;
     int id = idx[t];
     if (id >= 0 && id < N) atomicAdd(&count[(size_t)id + (size_t)N * (t / per_view)], 1u);
-}
-
-// exclusive scan of count (M entries) into offs (M + 1 entries), one block,
-// chunked: each of the 1024 threads scans a contiguous run
-__global__ void k_pixel_scan(size_t M, const unsigned* __restrict__ count, unsigned* __restrict__ offs) {
-    __shared__ unsigned part[1024];
-    size_t per = (M + blockDim.x - 1) / blockDim.x;
-    size_t lo = threadIdx.x * per, hi = min(M, lo + per);
-    unsigned s = 0;
-    for (size_t i = lo; i < hi; ++i) s += count[i];
-    part[threadIdx.x] = s;
-    __syncthreads();
-    for (int o = 1; o < (int)blockDim.x; o <<= 1) {
-        unsigned v = threadIdx.x >= (unsigned)o ? part[threadIdx.x - o] : 0;
-        __syncthreads();
-        part[threadIdx.x] += v;
-        __syncthreads();
-    }
-    unsigned run = threadIdx.x > 0 ? part[threadIdx.x - 1] : 0;
-    for (size_t i = lo; i < hi; ++i) {
-        offs[i] = run;
-        run += count[i];
-    }
-    if (threadIdx.x == blockDim.x - 1) offs[M] = part[threadIdx.x];
 }
 
 __global__ void k_pixel_place(size_t S, size_t per_view, int N, const int* __restrict__ idx,
@@ -142,7 +119,7 @@ extern "C" size_t uds_pixel_gather_workspace_size(int B, int W, int H, int K, in
     if (B <= 0 || W <= 0 || H <= 0 || K <= 0 || N < 0) return 0;
     size_t M = (size_t)B * N, S = (size_t)B * W * H * K;
     auto a = [](size_t x) { return (x + 255) & ~(size_t)255; };
-    return a(4 * M) * 2 + a(4 * (M + 1)) + a(4 * S);
+    return a(4 * M) * 2 + a(4 * (M + 1)) + a(4 * S) + a(4 * scan_part_entries(M));
 }
 
 extern "C" int uds_pixel_gather(int B, int W, int H, int K, const int32_t* indices, int N, int C,
@@ -167,11 +144,12 @@ extern "C" int uds_pixel_gather(int B, int W, int H, int K, const int32_t* indic
     unsigned* fill = reinterpret_cast<unsigned*>(p + a(4 * M));
     unsigned* offs = reinterpret_cast<unsigned*>(p + 2 * a(4 * M));
     unsigned* slots = reinterpret_cast<unsigned*>(p + 2 * a(4 * M) + a(4 * (M + 1)));
+    unsigned* part = reinterpret_cast<unsigned*>(p + 2 * a(4 * M) + a(4 * (M + 1)) + a(4 * S));
     cudaError_t e = cudaMemsetAsync(count, 0, 2 * a(4 * M), s);  // count and fill
     if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
     k_pixel_count<<<cdiv(S, 256), 256, 0, s>>>(S, per_view, N, indices, count);
-    k_pixel_scan<<<1, 1024, 0, s>>>(M, count, offs);
+    exclusive_scan(M, count, offs, part, s);
     k_pixel_place<<<cdiv(S, 256), 256, 0, s>>>(S, per_view, N, indices, offs, fill, slots);
     k_pixel_sum<<<cdiv(M, 128), 128, 0, s>>>(M, C, offs, slots, values, out);
-    return launch_status(4);
+    return launch_status(6);
 }
