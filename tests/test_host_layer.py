@@ -81,3 +81,24 @@ def test_room_scene_cameras_look_at_walls():
     assert sc["cam_positions"].shape == (4, 3)
     # every view sees a good share of the room in front of it
     assert ((pts[..., 2] < 0).float().mean(1) > 0.2).all()
+
+
+def test_lambert_expression_on_host_tensors():
+    """The renderer's Lambert keeps the reference's tensor expression for
+    operands the fused kernel does not take (here: host tensors); it equals
+    ambient * d + sum_l I_l clamp(<dir_l, n>, 0, 1) d / pi."""
+    from unbiased_differentiable_splatting_gb300.cudaExtensions import shading
+    from unbiased_differentiable_splatting_gb300.render import Lambert
+    g = torch.Generator().manual_seed(0)
+    B, N, L = 2, 50, 3
+    amb = 0.1 * torch.rand(1, 1, 3, generator=g)
+    dirs = torch.nn.functional.normalize(torch.randn(B, L, 3, generator=g), dim=-1)
+    inten = torch.rand(1, L, 3, generator=g)
+    nrm = torch.nn.functional.normalize(torch.randn(B, N, 3, generator=g), dim=-1)
+    dif = torch.rand(1, N, 3, generator=g)
+    assert shading.lambert_shapes(amb, dirs, inten, nrm, dif) is None
+    out = Lambert()(amb, dirs, inten, nrm, dif).double()
+    cos = torch.clamp(torch.einsum("blk,bnk->bln", dirs.double(), nrm.double()), 0.0, 1.0)
+    ref = amb.double() * dif.double() + torch.einsum("bln,lc,nc->bnc", cos, inten[0].double(),
+                                                     dif[0].double()) / math.pi
+    torch.testing.assert_close(out, ref, rtol=1e-5, atol=1e-6)
