@@ -16,7 +16,7 @@ gradients.  Metric: fwd+bwd Msamples/s (one sample = one (view, pixel, k)).
           loss inside the timed region;
 * roofline: the dominant kernel (the per-pixel descent) timed alone with
           CUDA events; algorithmic bytes = tree read once + indices written;
-* cpu_baseline: the CPU oracle (C, OpenMP) on a band of pixel rows.
+* cpu_baseline: the CPU oracle (C, OpenMP) on one whole view, FP64 direct and FP32.
 Multi-GPU (torchrun) runs independent replicas (the path has no exchange).
 """
 from __future__ import annotations
@@ -61,6 +61,11 @@ def make_scene(wl):
     if wl["scene"] == "harmonic":
         return scenes.harmonic_scene(n=wl["n"], sd_range=wl["sd_range"], width=wl["width"], seed=0)
     return scenes.sphere_scene(n=wl["n"], width=wl["width"], seed=0)
+
+
+# the config both arms print (the GPU arm flushes L2 between steps; the CPU
+# arm runs whole views that are far larger than any cache)
+L2_NOTE = "GPU arm: L2 flushed (256 MiB write) before each step; CPU arm: whole views, no flush"
 
 
 def workload_name(name, wl):
@@ -136,13 +141,20 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-def cpu_sample(wl, scene, target_s=12.0):
-    """The oracle (FP32 restatement of the reference, OpenMP over pixel rows)
-    on a bounded sample of the same workload: the full tree build of the view,
-    then descent + EWA / compositing / interpolation forward and backward on a
-    band of pixel rows sized to about `target_s` seconds.  The rate is scaled
-    to the whole image as S / (t_build + W * t_row).
-    Returns (Msamples/s, threads, description)."""
+def cpu_view(wl, scene, flavour):
+    """One whole view of the workload on the host CPU (the oracle: C, OpenMP
+    over pixel rows, all host threads): bandwidth, tree build, the sampling of
+    every pixel, then EWA weights, compositing and interpolation forward and
+    backward.  Nothing is scaled or extrapolated.
+
+    flavour "fp64": node masses as direct FP64 Gauss sums (the truncation
+    circles kept, no Hermite expansion) and FP64 descent arithmetic -- the
+    direct FP64 evaluation of the same estimator, the CPU baseline of a path
+    the reference runs only as CUDA kernels.  flavour "fp32": the reference's
+    algorithm in its own FP32 arithmetic with Hermite expansions, re-evaluated
+    per descent level as the reference's kernel does (the oracle the GPU
+    indices match bit for bit).
+    Returns (seconds, threads)."""
     import oracle
     from unbiased_differentiable_splatting_gb300 import scenes as S
     import torch
@@ -158,35 +170,42 @@ def cpu_sample(wl, scene, target_s=12.0):
     t0 = time.perf_counter()
     h = oracle.view_bandwidth(W, H, f, p, nb, sd, 0.0)
     r = oracle.cull_radius(h, prec)
-    tree = oracle.Tree(W, H, f, p, h, r, prec)
-    t_build = time.perf_counter() - t0
+    if flavour == "fp64":
+        tree = oracle.Tree(W, H, f, p, h, r, prec, coef_pool=0)  # no expansions are evaluated
+        idx = oracle.sample_fp64(tree, W, H, K, prec, seed=1)[None]
+    else:
+        tree = oracle.Tree(W, H, f, p, h, r, prec)
+        idx = tree.sample(W, H, K, prec, seed=1)[None]
+    w = oracle.splat_forward(W, H, f, idx, p[None], n[None], sd[None], 0.0)
+    dw = oracle.filter_forward(idx, w, W, H, f, p[None], n[None])
+    img = oracle.interp_forward(idx, dw, col)
+    gw, _ = oracle.interp_backward(np.ones_like(img), idx, dw, col)
+    gdw = oracle.filter_backward(idx, w, gw, W, H, f, p[None], n[None])
+    oracle.splat_backward(W, H, f, gdw, idx, p[None], n[None], sd[None], 0.0)
+    return time.perf_counter() - t0, oracle.num_threads()
 
-    def band(rows):
-        t0 = time.perf_counter()
-        x0 = (W - rows) // 2
-        idx = tree.sample(W, H, K, prec, seed=1, x0=x0, x1=x0 + rows)[None]
-        w = oracle.splat_forward(W, H, f, idx, p[None], n[None], sd[None], 0.0)
-        dw = oracle.filter_forward(idx, w, W, H, f, p[None], n[None])
-        img = oracle.interp_forward(idx, dw, col)
-        gw, _ = oracle.interp_backward(np.ones_like(img), idx, dw, col)
-        gdw = oracle.filter_backward(idx, w, gw, W, H, f, p[None], n[None])
-        oracle.splat_backward(W, H, f, gdw, idx, p[None], n[None], sd[None], 0.0)
-        return time.perf_counter() - t0
 
-    t4 = band(4)
-    t_empty = band(0)  # the per-image passes over empty pixels
-    per_row = max((t4 - t_empty) / 4, 1e-6)
-    rows = int(max(4, min(W, (target_s - t_build - t_empty) / per_row)))
-    t = band(rows)
-    per_row = max((t - t_empty) / rows, 1e-9)
-    t_full = t_build + t_empty + W * per_row
-    msps = W * H * K / t_full / 1e6
-    return msps, oracle.num_threads(), (f"full tree build ({t_build:.1f} s) + {rows} of {W} pixel rows of the "
-                                        f"{W}x{H} view ({t:.1f} s), scaled to the whole view")
+CPU_SAMPLE = {"fp64": "one whole {W}x{H} view: direct FP64 Gauss-sum masses, greedy descent and order sampling of "
+                      "every pixel, EWA / compositing / interpolation forward and backward",
+              "fp32": "one whole {W}x{H} view: the reference's FP32 algorithm with Hermite expansions (per-level "
+                      "re-evaluation), EWA / compositing / interpolation forward and backward"}
+
+
+def cpu_baseline(wl, scene):
+    """Both CPU flavours on one whole view each; `value` is the FP64 direct
+    evaluation (the faster of the two)."""
+    W = wl["width"]
+    S = W * W * wl["K"]
+    t64, thr = cpu_view(wl, scene, "fp64")
+    t32, _ = cpu_view(wl, scene, "fp32")
+    return {"value": S / t64 / 1e6, "unit": "Msamples/s", "cores": thr, "kind": "port",
+            "sample": CPU_SAMPLE["fp64"].format(W=W, H=W) + f" ({t64:.2f} s)", "arithmetic": "fp64",
+            "fp32_fgt": {"value": S / t32 / 1e6, "seconds": t32, "sample": CPU_SAMPLE["fp32"].format(W=W, H=W)}}
 
 
 def profiled_traffic(kernel="k_sample"):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary."""
+    """DRAM bytes per launch of `kernel` from the committed ncu summary of the
+    current build (the line `traffic_bytes_per_launch <kernel>: <bytes>`)."""
     path = os.path.join(ROOT, "profiles", "k_sample_harmonic500k_1024.md")
     try:
         for line in open(path):
@@ -198,25 +217,35 @@ def profiled_traffic(kernel="k_sample"):
 
 
 def reference_arm(args, wl, name):
+    """The reference's path on the host CPU: the direct FP64 evaluation of the
+    estimator on one whole view per step (the reference has no CPU execution
+    of this path).  Steps stop early, and say so, once the timed ones exceed
+    150 s."""
     rank, world, _ = dist_info()
     if rank != 0:
         return
     scene = make_scene(wl)
-    vals = []
-    desc = ""
+    W = wl["width"]
+    S = W * W * wl["K"]
     threads = 1
-    for i in range(args.warmup + args.steps):
-        v, threads, desc = cpu_sample(wl, scene, target_s=min(10.0, 60.0 / max(args.steps, 1)))
-        if i >= args.warmup:
-            vals.append(v)
-    value = float(np.median(vals))
+    for _ in range(min(args.warmup, 1)):
+        cpu_view(wl, scene, "fp64")
+    ts = []
+    t_start = time.perf_counter()
+    for _ in range(args.steps):
+        t, threads = cpu_view(wl, scene, "fp64")
+        ts.append(t)
+        if time.perf_counter() - t_start > 150.0:
+            break
+    t = float(np.median(ts))
+    value = S / t / 1e6
     print(json.dumps({
         "impl": "reference", "metric": "fwd+bwd Msamples/s", "value": value, "unit": "Msamples/s",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": workload_name(name, wl)},
+        "n_gpus": args.gpus, "steps": args.steps, "steps_timed": len(ts), "warmup": min(args.warmup, 1),
+        "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": workload_name(name, wl), "l2": L2_NOTE},
         "cpu_baseline": {"value": value, "unit": "Msamples/s", "cores": threads, "kind": "port",
-                         "sample": desc},
+                         "sample": CPU_SAMPLE["fp64"].format(W=W, H=W), "arithmetic": "fp64"},
         "e2e": {"value": value, "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
 
@@ -754,8 +783,7 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu:
         try:
-            v, thr, desc = cpu_sample(wl, scene)
-            cpu = {"value": v, "unit": "Msamples/s", "cores": thr, "kind": "port", "sample": desc}
+            cpu = cpu_baseline(wl, scene)
         except Exception as e:  # the CPU leg never decides the GPU result
             cpu = {"value": None, "unit": "Msamples/s", "cores": 0, "kind": "port", "sample": f"failed: {e}"}
 
@@ -764,10 +792,10 @@ def main():
             "metric": "fwd+bwd Msamples/s", "value": value, "unit": "Msamples/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": workload_name(args.workload, wl), "l2": "flushed (256 MiB write) before each step",
-                       "parallelism": f"replicas x{world}", "cuda_graph": graph is not None,
-                       "descent_tile": f"{tile}x{32 // tile} pixels per warp (autotuned: "
-                                       + ", ".join(f"{k}: {v:.3f} ms" for k, v in sorted(tile_ms.items())) + ")"},
+            "config": {"workload": workload_name(args.workload, wl), "l2": L2_NOTE},
+            "run": {"parallelism": f"replicas x{world}", "cuda_graph": graph is not None,
+                    "descent_tile": f"{tile}x{32 // tile} pixels per warp (autotuned: "
+                                    + ", ".join(f"{k}: {v:.3f} ms" for k, v in sorted(tile_ms.items())) + ")"},
             "e2e": {"value": e2e, "unit": "Msamples/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": 4,
                     "path": ("pinned H2D into the captured step's inputs + CUDA-graph replay of Splatting fwd+bwd "
                              "+ loss D2H" if graph is not None else "pinned H2D + Splatting fwd+bwd + loss D2H"),

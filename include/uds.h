@@ -272,9 +272,11 @@ int uds_splat_backward(int B, int W, int H, int K, float focal, const float* gra
  * not allocate after start-up).  No counterpart in the reference.  Same
  * arguments and results as uds_splat_forward minus the workspace; the scratch
  * is a fixed 8 MiB array inside the library, so B*N must not exceed 262144
- * (larger calls return UDS_ERR_ARGUMENT).  The first call on a device looks
- * the array up (make it before any stream capture); calls that overlap on the
- * GPU share the array and race. */
+ * (larger calls return UDS_ERR_ARGUMENT).  Every call looks the array's
+ * device address up on the current device, so a device reset between calls
+ * is harmless; the first call on a device may load the library's device code
+ * (make it before any stream capture); calls that overlap on the GPU share
+ * the array and race. */
 int uds_splat_forward_static(int B, int W, int H, int K, float focal, const int32_t* indices,
                              const float* points, const float* normals, int std_batch, int N,
                              const float* std_devs, float smoothing, float* weights, void* stream);

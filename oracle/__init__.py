@@ -204,6 +204,21 @@ def interp_forward(idx, w, attr):
     return out
 
 
+def chain64_forward(W, H, f, idx, pts, nrm, sd, smoothing, attr):
+    """EWA -> compositing -> interpolation of one view in FP64 for fixed
+    indices (W,H,K); pts/nrm (N,3), sd (N,2), attr (N,C) -> image (W,H,C)
+    float64."""
+    idx = _i(idx)
+    d = lambda a: np.ascontiguousarray(a, dtype=np.float64)  # noqa: E731
+    pts, nrm, sd, attr = d(pts), d(nrm), d(sd), d(attr)
+    K = idx.shape[-1]
+    Cn = attr.shape[1]
+    img = np.zeros((W, H, Cn), np.float64)
+    lib().orc_chain64_forward(C(W), C(H), C(K), ctypes.c_double(f), P(idx), C(pts.shape[0]), P(pts), P(nrm), P(sd),
+                              ctypes.c_double(smoothing), C(Cn), P(attr), P(img))
+    return img
+
+
 def interp_backward(gin, idx, w, attr):
     gin, idx, w, attr = _f(gin), _i(idx), _f(w), _f(attr)
     B, W, H, K = idx.shape
@@ -364,6 +379,19 @@ class Tree:
         if st != 0:
             raise RuntimeError("oracle sampler trace overflow")
         return idx
+
+
+def sample_fp64(tree, W, H, K, precision, seed=0, view=0, x0=0, x1=None):
+    """The estimator evaluated directly in FP64 on an oracle Tree (direct Gauss
+    sums instead of Hermite expansions; same descent and order sampling with
+    Philox uniforms): indices (W,H,K)."""
+    idx = np.full((W, H, K), -1, np.int32)
+    st = lib().orc_tree_sample_fp64(ctypes.c_void_p(tree.ptr), C(W), C(H), C(K), ctypes.c_double(precision),
+                                    ctypes.c_uint64(seed), ctypes.c_uint32(view), C(x0), C(W if x1 is None else x1),
+                                    P(idx))
+    if st != 0:
+        raise RuntimeError("oracle FP64 sampler: path deeper than 64 levels")
+    return idx
 
 
 def sample_view_stochastic(W, H, f, pts, nrm, sd, K, smoothing, precision, h=0.0, seed=0, view=0, flavour=DET):

@@ -585,6 +585,86 @@ void orc_interp_backward(int B, int W, int H, int K, const float* gin, const int
 }
 
 /* ------------------------------------------------------------------------
+ * The EWA -> compositing -> interpolation chain in FP64 for fixed indices:
+ * the reference for central differences of the CUDA backward kernels.  The
+ * formulas are those of the FP32 functions above, every operation in double:
+ * the weight (ewaSplatting.cuh:8-91, clamped at 1 as ewaSplatting.cuh:90),
+ * the signed distance along the pixel ray (alphacompositing.cuh:6-30), the
+ * stable insertion sort (alphacompositing.cuh:32-56), the front-to-back blend
+ * (alphacompositing.cuh:58-68) and the weighted attribute sum
+ * (interpolationCuda.cu:5-46).
+ * ---------------------------------------------------------------------- */
+static double ewa_weight64(const double* pixel, double W, double H, double F, const double* p, const double* n,
+                           const double* sd, double sm) {
+    double s0 = -(p[0] * F) / p[2] + W / 2.0, s1 = (p[1] * F) / p[2] + H / 2.0;
+    double a0 = (W - 2.0 * s0) / (2.0 * F), a1 = -(H - 2.0 * s1) / (2.0 * F);
+    double x0[3] = {a0 - 1.0 / F, a1, 1.0}, x1[3] = {a0, a1 + 1.0 / F, 1.0};
+    double c = dot3d(p, n);
+    double k0 = c / dot3d(x0, n), k1 = c / dot3d(x1, n);
+    double t0[3], t1[3];
+    for (int i = 0; i < 3; ++i) { t0[i] = k0 * x0[i] - p[i]; t1[i] = k1 * x1[i] - p[i]; }
+    double al = sqrt(dot3d(t0, t0));
+    double u0[3] = {t0[0] / al, t0[1] / al, t0[2] / al}, u1[3];
+    cross3d(u0, n, u1);
+    double be = dot3d(t1, u0), ga = dot3d(t1, u1);
+    double J00 = 1.0 / al, J01 = -be / (al * ga), J11 = 1.0 / ga;
+    double S0 = sd[0] * sd[0], S1 = sd[1] * sd[1];
+    double V00 = J00 * J00 * S0 + J01 * J01 * S1 + sm, V01 = J01 * J11 * S1, V11 = J11 * J11 * S1 + sm;
+    double vdet = V00 * V11 - V01 * V01;
+    double d0 = pixel[0] - s0, d1 = pixel[1] - s1;
+    double e = (d0 * (V11 * d0 - V01 * d1) + d1 * (V00 * d1 - V01 * d0)) / vdet;
+    double G = exp(-0.5 * e) / (2.0 * ORC_PI * sqrt(vdet) * fabs(al * ga));
+    return G < 1.0 ? G : 1.0;
+}
+
+void orc_chain64_forward(int W, int H, int K, double f, const int* idx, int N, const double* pts,
+                         const double* nrm, const double* sd, double smoothing, int C, const double* attr,
+                         double* img) {
+    (void)N;
+#pragma omp parallel for schedule(static)
+    for (long long pix = 0; pix < (long long)W * H; ++pix) {
+        int i = (int)(pix / H), j = (int)(pix % H);
+        double pixel[2] = {(double)i, (double)j};
+        const int* ix = &idx[(size_t)K * pix];
+        double w[64], dist[64], out[64];
+        int ord[64];
+        double wd[3] = {((double)W - 2.0 * i) / (2.0 * f), -((double)H - 2.0 * j) / (2.0 * f), 1.0};
+        double nw = sqrt(dot3d(wd, wd));
+        double dir[3] = {-wd[0] / nw, -wd[1] / nw, -wd[2] / nw};
+        for (int k = 0; k < K; ++k) {
+            w[k] = 0.0;
+            dist[k] = (double)ORC_ZMAX;
+            int id = ix[k];
+            if (id < 0) continue;
+            const double* p = &pts[3 * (size_t)id];
+            const double* n = &nrm[3 * (size_t)id];
+            w[k] = ewa_weight64(pixel, W, H, f, p, n, &sd[2 * (size_t)id], smoothing);
+            double d = dot3d(p, n) / dot3d(dir, n);
+            if (d > 0.0) dist[k] = d;
+        }
+        for (int k = 0; k < K; ++k) ord[k] = k;
+        for (int k = 1; k < K; ++k) {
+            int index = ord[k];
+            int m = k;
+            while (m > 0 && dist[ord[m - 1]] > dist[index]) { ord[m] = ord[m - 1]; --m; }
+            ord[m] = index;
+        }
+        double rem = 1.0;
+        for (int k = 0; k < K; ++k) {
+            out[ord[k]] = rem * w[ord[k]];
+            rem *= 1.0 - w[ord[k]];
+        }
+        double* o = &img[(size_t)C * pix];
+        for (int c = 0; c < C; ++c) o[c] = 0.0;
+        for (int k = 0; k < K; ++k) {
+            int id = ix[k];
+            if (id < 0) continue;
+            for (int c = 0; c < C; ++c) o[c] += out[k] * attr[(size_t)C * id + c];
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------
  * Shading (diffuseShading.cuh, diffuseShadingGrad.cuh, shadingCuda.cu)
  * ---------------------------------------------------------------------- */
 void orc_shade_forward(int B, int P, int L, const float* dirs, const float* I, int IB,
@@ -1270,6 +1350,107 @@ int orc_tree_sample(const orc_tree* t, int W, int H, int K, float precision, con
                     int leafNode = n - 1 + f0 + k;
                     float pw = fmaxf(0.0f, orc_tree_node_weight(t, leafNode, q, fl));
                     insert_sample(t->ids[f0 + k], u[k] / pw, out, keys, K);
+                }
+            }
+        }
+    }
+    return status;
+}
+
+/* The same estimator evaluated directly in FP64 (the CPU baseline the
+ * reference lacks): node masses are sums of exp(-|q - y|^2 / (2 h^2)) over
+ * the node's leaves in double, skipping subtrees whose box misses the
+ * node's truncation circle (the truncation of getWeight,
+ * evaluateDynamicRadixTree.cuh:118-126) but using no Hermite expansion; the
+ * greedy descent, the capacities and the order-sampling keys follow
+ * orc_tree_sample in double. */
+static double direct_trunc64(const orc_tree* t, int node, const double* q) {
+    int stack[ORC_STACK + 2];
+    int sp = 0;
+    double s = 0.0, i2h2 = 1.0 / (2.0 * (double)t->h * (double)t->h);
+    stack[sp++] = node;
+    while (sp) {
+        int v = stack[--sp];
+        if (v >= t->n - 1) {
+            int i = v - (t->n - 1);
+            double dx = q[0] - t->leafxy[2 * i], dy = q[1] - t->leafxy[2 * i + 1];
+            s += exp(-(dx * dx + dy * dy) * i2h2);
+            continue;
+        }
+        double cx = fmin(fmax(q[0], t->box[4 * v]), t->box[4 * v + 2]);
+        double cy = fmin(fmax(q[1], t->box[4 * v + 1]), t->box[4 * v + 3]);
+        double r = t->trunc[v];
+        if ((q[0] - cx) * (q[0] - cx) + (q[1] - cy) * (q[1] - cy) >= r * r) continue;
+        if (sp + 2 > ORC_STACK + 2) return s;  /* deeper than any tree built here */
+        stack[sp++] = t->right[v];
+        stack[sp++] = t->left[v];
+    }
+    return s;
+}
+
+int orc_tree_sample_fp64(const orc_tree* t, int W, int H, int K, double precision, uint64_t seed, uint32_t view,
+                         int x0, int x1, int* indices) {
+    int R = orc_num_rounds(K);
+    int n = t->n;
+    int status = 0;
+    if (x1 > W) x1 = W;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int i = x0; i < x1; ++i) {
+        int tnode[8][ORC_STACK];
+        double tprob[8][ORC_STACK], tcap[8][ORC_STACK];
+        int tlen[8];
+        double keys[64];
+        float u[64];
+        for (int j = 0; j < H; ++j) {
+            size_t pixel = (size_t)j + (size_t)H * i;
+            int* out = &indices[(size_t)K * pixel];
+            for (int k = 0; k < K; ++k) { out[k] = -1; keys[k] = INFINITY; }
+            if (n == 0) continue;
+            double q[2] = {(double)i, (double)j};
+            if (direct_trunc64(t, 0, q) < precision) continue;
+            for (int r = 0; r < R && r < 8; ++r) {
+                orc_philox_uniforms(seed, view, (uint32_t)pixel, (uint32_t)r, K, u);
+                int v = 0, d = 0;
+                tnode[r][0] = 0; tprob[r][0] = 1.0;
+                while (t->count[v] > K) {
+                    int a = t->left[v], b = t->right[v];
+                    double w0 = direct_trunc64(t, a, q), w1 = direct_trunc64(t, b, q);
+                    double sum = w0 + w1;
+                    w0 /= sum; w1 /= sum;
+                    double c0 = 1.0, c1 = 1.0;
+                    for (int rr = r - 1; rr >= 0; --rr)
+                        if (d + 1 < tlen[rr] && tnode[rr][d + 1] == a) { c0 = tcap[rr][d + 1]; break; }
+                    for (int rr = r - 1; rr >= 0; --rr)
+                        if (d + 1 < tlen[rr] && tnode[rr][d + 1] == b) { c1 = tcap[rr][d + 1]; break; }
+                    double s0 = w0 * c0, s1 = w1 * c1;
+                    ++d;
+                    if (d >= ORC_STACK) { status = -1; break; }
+                    if (s0 < s1) { tnode[r][d] = b; tprob[r][d] = w1; v = b; }
+                    else { tnode[r][d] = a; tprob[r][d] = w0; v = a; }
+                }
+                if (d >= ORC_STACK) break;
+                tlen[r] = d + 1;
+                double prob = 1.0;
+                for (int m = d; m >= 0; --m) {
+                    double cap = 1.0;
+                    for (int rr = r - 1; rr >= 0; --rr)
+                        if (m < tlen[rr] && tnode[rr][m] == tnode[r][m]) { cap = tcap[rr][m]; break; }
+                    tcap[r][m] = fmax(0.0, cap - prob);
+                    prob *= tprob[r][m];
+                }
+                int c = t->count[v], f0 = t->first[v];
+                for (int k = 0; k < c; ++k) {
+                    double dx = q[0] - t->leafxy[2 * (f0 + k)], dy = q[1] - t->leafxy[2 * (f0 + k) + 1];
+                    double pw = exp(-(dx * dx + dy * dy) / (2.0 * (double)t->h * (double)t->h));
+                    double key = (double)u[k] / pw;
+                    int index = t->ids[f0 + k];
+                    for (int s = 0; s < K; ++s) {
+                        if (key < keys[s]) {
+                            int ti = out[s]; out[s] = index; index = ti;
+                            double tk = keys[s]; keys[s] = key; key = tk;
+                        }
+                        if (index == -1) break;
+                    }
                 }
             }
         }

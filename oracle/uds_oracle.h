@@ -74,6 +74,12 @@ void orc_interp_backward(int B, int W, int H, int K, const float* gin, const int
                          const float* w, int aB, int N, int C, const float* attr, float* gw,
                          float* ga);
 
+/* EWA weight -> compositing -> interpolation for one view and fixed indices,
+ * every operation in double (central-difference reference; sd (N,2), attr (N,C)) */
+void orc_chain64_forward(int W, int H, int K, double f, const int* idx, int N, const double* pts,
+                         const double* nrm, const double* sd, double smoothing, int C, const double* attr,
+                         double* img);
+
 /* pixelgather (pixelGatherCuda.cu:7-152): scatter (B,N,C) -> (B,W,H,K,C);
  * gather (B,W,H,K,C) -> (B,N,C), each splat's samples summed in sample order */
 void orc_pixel_scatter(int B, int W, int H, int K, const int* idx, int N, int C, const float* values,
@@ -132,6 +138,11 @@ double orc_tree_direct_weight(const orc_tree* t, int node, const double* query);
  * indices is the full W*H*K array.  Returns 0, or -1 on trace overflow. */
 int orc_tree_sample(const orc_tree* t, int W, int H, int K, float precision, const float* uniforms,
                     uint64_t seed, uint32_t view, int x0, int x1, int flavour, int* indices);
+/* the same estimator with direct FP64 Gauss sums for the node masses (no
+ * Hermite expansion; the truncation circles are kept) and FP64 descent
+ * arithmetic: the CPU baseline of the whole view */
+int orc_tree_sample_fp64(const orc_tree* t, int W, int H, int K, double precision, uint64_t seed, uint32_t view,
+                         int x0, int x1, int* indices);
 
 /* Stochastic mode: K independent mass-proportional descents per pixel;
  * indices (W*H*K) and path probabilities probs (W*H*K). */

@@ -1,12 +1,14 @@
 """Generate the golden fixtures of tests/golden/ from the reference itself.
 
 The reference shim oracle/_ref/libudsref.so is compiled (``make -C oracle
-ref``) from the reference's own headers where they lie in the reference
-checkout; this script calls those functions on seeded synthetic inputs and
-stores inputs and outputs as compressed .npz files.  It is run by hand in a
-container that has the reference checkout; the fixtures are committed so the
-tests need neither the reference nor the shim.
+ref``, with UDS_REFERENCE_DIR naming the reference checkout) from the
+reference's own headers where they lie in that checkout; this script calls
+those functions on seeded synthetic inputs and stores inputs and outputs as
+compressed .npz files.  It is run by hand where the reference checkout
+exists; the fixtures are committed so the tests need neither the reference
+nor the shim.
 
+    UDS_REFERENCE_DIR=<checkout> make -C oracle ref
     python tests/golden/make_golden.py
 """
 from __future__ import annotations

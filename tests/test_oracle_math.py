@@ -293,3 +293,30 @@ def test_nearest_samples_oracle_brute_force():
                    for c in cands[s])
         want = [c for _, c in d[:M]] + [-1] * max(0, M - len(d))
         assert list(got[s]) == want, (s, list(got[s]), want)
+
+
+def test_chain64_matches_fp32_chain():
+    """The FP64 chain (central-difference reference of the GPU tests) against
+    the FP32 restatement it mirrors: EWA weights, compositing and
+    interpolation of the same fixed indices agree to FP32 precision."""
+    rng = np.random.default_rng(12)
+    W = H = 20
+    f, K, N = 18.0, 4, 50
+    z = rng.uniform(-2.2, -1.8, N)
+    pts = np.stack([rng.uniform(-0.45, 0.45, N) * (-z) * W / f, rng.uniform(-0.45, 0.45, N) * (-z) * H / f, z], 1)
+    n = rng.normal(size=(N, 3))
+    n[:, 2] = np.abs(n[:, 2]) + 1.5
+    n /= np.linalg.norm(n, axis=1, keepdims=True)
+    sd = rng.uniform(0.4, 0.7, size=(N, 2))
+    col = rng.uniform(0.2, 1.0, size=(N, 3))
+    pts, n, sd, col = (a.astype(np.float32) for a in (pts, n, sd, col))
+    sx = -(pts[:, 0] * f) / pts[:, 2] + W / 2
+    sy = (pts[:, 1] * f) / pts[:, 2] + H / 2
+    gi, gj = np.meshgrid(np.arange(W), np.arange(H), indexing="ij")
+    idx = np.argsort((gi[..., None] - sx) ** 2 + (gj[..., None] - sy) ** 2, axis=-1)[..., :K].astype(np.int32)
+    idx[0, 0, 1] = -1  # an empty slot
+    w = oracle.splat_forward(W, H, f, idx[None], pts[None], n[None], sd[None], 0.0)
+    dw = oracle.filter_forward(idx[None], w, W, H, f, pts[None], n[None])
+    img32 = oracle.interp_forward(idx[None], dw, col[None])[0]
+    img64 = oracle.chain64_forward(W, H, f, idx, pts, n, sd, 0.0, col)
+    assert np.abs(img64 - img32).max() < 1e-5 * max(np.abs(img64).max(), 1.0)

@@ -73,3 +73,48 @@ def test_static_rejects_more_than_its_array(L):
                                     dummy.data_ptr(), 0.0, dummy.data_ptr(), torch.cuda.current_stream().cuda_stream)
     assert st == 1
     assert b"262144" in L.uds_last_error()
+
+
+def test_static_allocates_nothing(L):
+    """After one warm call, a second call changes neither torch's allocator
+    nor the device's free memory."""
+    W, H, K, f, B, N = 32, 24, 4, 30.0, 2, 2000
+    idx, pts, nrm, sd = _inputs(3, B, N, W, H, K, f)
+    out = torch.empty(idx.shape, dtype=torch.float32, device=DEV)
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def call():
+        st = L.uds_splat_forward_static(B, W, H, K, f, idx.data_ptr(), pts.data_ptr(), nrm.data_ptr(), 1, N,
+                                        sd.data_ptr(), 0.0, out.data_ptr(), stream)
+        assert st == 0, L.uds_last_error()
+        torch.cuda.synchronize()
+
+    call()
+    before = (torch.cuda.memory_allocated(), torch.cuda.mem_get_info()[0])
+    call()
+    after = (torch.cuda.memory_allocated(), torch.cuda.mem_get_info()[0])
+    assert after == before
+
+
+def test_static_per_view_std_devs_and_no_splats(L):
+    """std_batch = B (per-view std-devs) against the workspace entry point,
+    and N = 0: every weight is zero."""
+    W, H, K, f, B, N = 40, 32, 8, 36.0, 3, 1500
+    stream = torch.cuda.current_stream().cuda_stream
+    idx, pts, nrm, _ = _inputs(4, B, N, W, H, K, f)
+    sd = torch.as_tensor(np.random.default_rng(4).uniform(0.008, 0.03, size=(B, N, 2)).astype(np.float32)).to(DEV)
+    ws = torch.empty(L.uds_splat_workspace_size(B, N), dtype=torch.uint8, device=DEV)
+    ref = torch.empty(idx.shape, dtype=torch.float32, device=DEV)
+    assert L.uds_splat_forward(B, W, H, K, f, idx.data_ptr(), pts.data_ptr(), nrm.data_ptr(), B, N, sd.data_ptr(),
+                               0.0, ref.data_ptr(), ws.data_ptr(), ws.numel(), stream) == 0
+    out = torch.full(idx.shape, float("nan"), dtype=torch.float32, device=DEV)
+    assert L.uds_splat_forward_static(B, W, H, K, f, idx.data_ptr(), pts.data_ptr(), nrm.data_ptr(), B, N,
+                                      sd.data_ptr(), 0.0, out.data_ptr(), stream) == 0, L.uds_last_error()
+    torch.cuda.synchronize()
+    assert _rel_l2(out, ref) < 1e-6
+    empty = torch.full((1, W, H, K), -1, dtype=torch.int32, device=DEV)
+    out0 = torch.full((1, W, H, K), float("nan"), dtype=torch.float32, device=DEV)
+    assert L.uds_splat_forward_static(1, W, H, K, f, empty.data_ptr(), 0, 0, 1, 0, 0, 0.0, out0.data_ptr(),
+                                      stream) == 0, L.uds_last_error()
+    torch.cuda.synchronize()
+    assert torch.all(out0 == 0)

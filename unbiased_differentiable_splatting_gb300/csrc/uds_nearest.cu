@@ -103,6 +103,8 @@ extern "C" int uds_nearest_samples(int B, int W, int H, int K, const int32_t* in
         !indices || !weights || (N > 0 && (!points || !nearest)))
         return UDS_ERR_ARGUMENT;
     if (N == 0) return UDS_OK;
+    // pair counts, offsets and the scan are 32-bit
+    if ((size_t)B * W * H * K >= (1ull << 32)) return UDS_ERR_ARGUMENT;
     if (!workspace || workspace_bytes < uds_nearest_workspace_size(B, W, H, K, N)) return UDS_ERR_WORKSPACE;
     cudaStream_t s = as_stream(stream);
     auto a = [](size_t x) { return (x + 255) & ~(size_t)255; };

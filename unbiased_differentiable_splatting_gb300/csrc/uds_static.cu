@@ -15,21 +15,20 @@
 //    uds_last_error();
 //  - the array occupies 8 MiB on every GPU that loads this library, until the
 //    process exits;
-//  - the first call on a device looks up the array's device address
-//    (cudaGetSymbolAddress) with that device current; make that first call
-//    before any stream capture;
+//  - every call asks the runtime for the array's device address on the
+//    current device (cudaGetSymbolAddress, a host-side query, with its return
+//    code checked), so the address is never stale, also not after a device
+//    reset; the first call on a device may load the library's device code,
+//    so make that first call before any stream capture;
 //  - every call uses the same array: calls that overlap on the GPU (different
 //    streams, or different host threads without ordering) race on it.
 //    Nothing in it needs to start at zero: each call writes the constants of
 //    all its splats before reading any.
-#include <mutex>
-
 #include "uds_ewa.cuh"
 
 namespace uds {
 
 constexpr int kStaticMaxSplats = 1 << 18;
-constexpr int kStaticMaxDevices = 64;
 
 // Two float4 of Gaussian constants per (view, splat) pair.
 static __device__ __align__(256) float4 g_splat_scratch[2 * kStaticMaxSplats];
@@ -75,26 +74,15 @@ __global__ void k_static_forward(int B, int W, int H, int K, const int* __restri
     }
 }
 
-// Device address of the scratch array on the current device, looked up once
-// per device (host code cannot use the array's name as a device pointer).
+// Device address of the scratch array on the current device.  Host code
+// cannot use the array's name as a device pointer (it names a host-side
+// stand-in), so the address comes from the runtime, asked on every call with
+// the caller's device current.
 static int scratch_address(float4** out) {
-    static std::mutex mu;
-    static float4* addr[kStaticMaxDevices] = {};
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_splat_scratch);
     if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
-    if (dev < 0 || dev >= kStaticMaxDevices) {
-        set_last_error_message("device ordinal beyond the static scratch table");
-        return UDS_ERR_ARGUMENT;
-    }
-    std::lock_guard<std::mutex> lock(mu);
-    if (!addr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_splat_scratch);
-        if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
-        addr[dev] = reinterpret_cast<float4*>(p);
-    }
-    *out = addr[dev];
+    *out = reinterpret_cast<float4*>(p);
     return UDS_OK;
 }
 

@@ -68,8 +68,12 @@ LAMBERT_MAX_LIGHTS = 4
 def lambert_shapes(ambient, directions, intensities, normals, diffuse):
     """(B, N, L, aB, IB, dB) when the operands have the shapes the fused
     kernel takes, else None: normals (B, N, 3), diffuse (dB, N, 3), directions
-    (B, L, 3), intensities (IB, L, 3), ambient (aB, 1, 3), (aB, 3) or (3,),
-    with dB, IB, aB in {1, B}, float32 CUDA tensors on one device."""
+    (B, L, 3), intensities (IB, L, 3), ambient (aB, 1, 3) with aB in {1, B},
+    or (1, 3) or (3,); dB, IB in {1, B}; float32 CUDA tensors on one device.
+    A 2-D ambient with more than one row broadcasts against the splat axis in
+    the reference's expression ``ambientLight * diffuse`` (one ambient per
+    splat when it has N rows, an error otherwise), so it is left to that
+    expression."""
     ts = (ambient, directions, intensities, normals, diffuse)
     if not all(isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float32 for t in ts):
         return None
@@ -84,9 +88,16 @@ def lambert_shapes(ambient, directions, intensities, normals, diffuse):
     if diffuse.dim() != 3 or tuple(diffuse.shape[1:]) != (N, 3):
         return None
     IB, dB = intensities.shape[0], diffuse.shape[0]
-    if ambient.shape[-1] != 3 or any(s != 1 for s in ambient.shape[1:-1]):
+    if ambient.shape[-1] != 3 or ambient.dim() > 3:
         return None
-    aB = ambient.shape[0] if ambient.dim() >= 2 else 1
+    if ambient.dim() == 3:
+        if ambient.shape[1] != 1:
+            return None
+        aB = ambient.shape[0]
+    else:
+        if ambient.dim() == 2 and ambient.shape[0] != 1:
+            return None
+        aB = 1
     if any(x not in (1, B) for x in (IB, dB, aB)):
         return None
     return B, N, L, aB, IB, dB
