@@ -99,6 +99,18 @@ int uds_view_matrix_forward(int B, const float* positions, const float* quaterni
 int uds_view_matrix_backward(int B, const float* grad, const float* quaternions, float* grad_positions,
                              float* grad_quaternions, void* stream);
 
+/* ---- BackfaceCulling (render.py:193-205, a tensor expression in the
+ *      reference): splats whose camera-space normal has z > 0 get the
+ *      camera-space normal and, when normals is given, the world normal
+ *      negated.  cam_normals, flipped_cam (B,N,3); normals (nB,N,3), nB in
+ *      {1, B}, flipped_normals (B,N,3) (both may be NULL).  Backward: the
+ *      flips of the two incoming gradients (either may be NULL); grad_normals
+ *      (nB,N,3), summed over the views in view order when nB == 1. ---- */
+int uds_backface_forward(int B, int N, const float* cam_normals, int nB, const float* normals, float* flipped_cam,
+                         float* flipped_normals, void* stream);
+int uds_backface_backward(int B, int N, const float* cam_normals, const float* grad_flipped_cam, int nB,
+                          const float* grad_flipped_normals, float* grad_cam, float* grad_normals, void* stream);
+
 /* ---- sampling.sample (sampling.cpp:48-94): points, normals (B,N,3)
  *      camera space, stdDevs (std_batch,N,2) -> indices (B,W,H,K) int32,
  *      -1 where no sample.  uniforms: optional (B,W,H,R,K) float32 in (0,1],
@@ -196,6 +208,20 @@ size_t uds_nearest_workspace_size(int B, int W, int H, int K, int N);
 int uds_nearest_samples(int B, int W, int H, int K, const int32_t* indices, const float* weights, int N,
                         const float* points, int num_nearest, int32_t* nearest, void* workspace,
                         size_t workspace_bytes, void* stream);
+
+/* ---- NearestSamplesRegularizer.forward (splatting/regularizier.py:119-175)
+ *      over the nearest lists of uds_nearest_samples: nearest (N,M) int32
+ *      (-1 padded; index 0 is masked like the reference's `nearest > 0`),
+ *      points / normals (1,N,3).  losses[0] = normal loss, losses[1] = plane
+ *      loss, summed over splats (mean != 0: divided by N); grad_points /
+ *      grad_normals (N,3) = their gradients w.r.t. the splat's own point
+ *      (plane loss) and normal (normal loss), the neighbour weights and the
+ *      filtered normals held constant as in the reference.  Deterministic.
+ *      Workspace: uds_nearest_regularizer_workspace_size(N) bytes. ---- */
+size_t uds_nearest_regularizer_workspace_size(int N);
+int uds_nearest_regularizer(int N, int M, const int32_t* nearest, const float* points, const float* normals,
+                            float sigma, int mean, float* losses, float* grad_points, float* grad_normals,
+                            void* workspace, size_t workspace_bytes, void* stream);
 
 /* ---- training-step tail (optimization_geometry.py:190-219), fused.
  *      uds_image_loss: kind 0 = L1, 1 = L2 (losses.py:5-31); *loss =

@@ -33,7 +33,33 @@ def test_nearest_matches_oracle(ns, M):
     assert (ref >= 0).any()
 
 
-def test_regularizer_on_render(ns):
+def _regularizer_fp64(nearest, pts, nrm, sigma):
+    """NearestSamplesRegularizer (regularizier.py:119-175) restated in FP64
+    numpy: per-splat normal and plane losses, and their gradients w.r.t. the
+    splat's own normal and point (weights and mean normals held constant)."""
+    n = nearest[0]
+    P = pts[0].astype(np.float64)
+    Nn = nrm[0].astype(np.float64)
+    mask = (n > 0)[..., None].astype(np.float64)
+    j = np.clip(n, 0, None)
+    Pj, Nj = P[j], Nn[j]
+    gauss = lambda x: np.exp(-x ** 2 / sigma ** 2)  # noqa: E731
+    w = mask * gauss(np.linalg.norm(Nn[:, None] - Nj, axis=-1))[..., None] * \
+        gauss(np.linalg.norm(P[:, None] - Pj, axis=-1))[..., None]
+    inv = 1.0 / (w.sum(1) + 1e-4)
+    F = (w * Nj).sum(1)
+    filt = F / (np.linalg.norm(F, axis=-1, keepdims=True) + 1e-4)
+    pm = np.clip(mask.sum(1), 0, 1)
+    D = (w * ((P[:, None] - Pj) * Nj).sum(-1, keepdims=True)).sum(1)
+    plane = (inv * D) ** 2
+    normal = pm * ((filt - Nn) ** 2).sum(-1, keepdims=True)
+    return normal[:, 0], plane[:, 0], 2 * inv ** 2 * D * F, -2 * pm * (filt - Nn)
+
+
+@pytest.mark.parametrize("reduction", ["sum", "mean"])
+def test_regularizer_on_render(ns, reduction):
+    """The regulariser's kernel on a rendered view's nearest lists against the
+    FP64 restatement: both losses and the points' / normals' gradients."""
     from unbiased_differentiable_splatting_gb300 import scenes
     from unbiased_differentiable_splatting_gb300.regularizers import NearestSamplesRegularizer
     from unbiased_differentiable_splatting_gb300.render import RenderOptions, Splatting
@@ -44,8 +70,19 @@ def test_regularizer_on_render(ns):
     nrm = d["normals"].clone().requires_grad_(True)
     img, idx, dw = r(d["cam_positions"], d["cam_orientations"], pts, nrm, d["stddevs"], d["colors"], d["ambient"],
                      d["lamp_directions"], d["lamp_intensities"])
-    reg = NearestSamplesRegularizer(sigma=0.5, num_nearest=10)
+    reg = NearestSamplesRegularizer(sigma=0.5, num_nearest=10, reduction=reduction)
+    pts.grad = nrm.grad = None
     ln, lp = reg(idx, dw, pts, nrm)
-    (ln + lp).backward()
-    assert torch.isfinite(ln) and torch.isfinite(lp) and float(ln.detach()) > 0
-    assert torch.isfinite(pts.grad).all() and pts.grad.abs().sum() > 0
+    (0.5 * ln + 2.0 * lp).backward()
+    nearest = ns.nearest(idx, dw.detach().contiguous(), pts.detach().contiguous(), 10).cpu().numpy()
+    rn, rp, gp, gn = _regularizer_fp64(nearest, pts.detach().cpu().numpy(), nrm.detach().cpu().numpy(), 0.5)
+    N = rn.shape[0]
+    s = 1.0 / N if reduction == "mean" else 1.0
+    assert (nearest > 0).any() and rn.sum() > 0
+    np.testing.assert_allclose(float(ln), rn.sum() * s, rtol=1e-5)
+    np.testing.assert_allclose(float(lp), rp.sum() * s, rtol=1e-4, atol=1e-9)
+    for got, ref in ((pts.grad, 2.0 * s * gp), (nrm.grad, 0.5 * s * gn)):
+        got = got.cpu().numpy()[0].astype(np.float64)
+        assert np.linalg.norm(got - ref) <= 1e-5 * np.linalg.norm(ref) + 1e-12
+    with pytest.raises(ValueError):
+        NearestSamplesRegularizer(reduction="max")(idx, dw, pts, nrm)

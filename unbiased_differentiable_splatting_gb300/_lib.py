@@ -43,6 +43,9 @@ _SIGS = {
                                        c_void_p, c_void_p]),
     "uds_view_matrix_forward": (c_int, [c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "uds_view_matrix_backward": (c_int, [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "uds_backface_forward": (c_int, [c_int, c_int, c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "uds_backface_backward": (c_int, [c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p,
+                                      c_void_p]),
     "uds_sample_workspace_size": (c_size_t, [ctypes.POINTER(SampleParams)]),
     "uds_sample": (c_int, [ctypes.POINTER(SampleParams), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                            c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
@@ -76,6 +79,9 @@ _SIGS = {
     "uds_nearest_workspace_size": (c_size_t, [c_int, c_int, c_int, c_int, c_int]),
     "uds_nearest_samples": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_int,
                                     c_void_p, c_void_p, c_size_t, c_void_p]),
+    "uds_nearest_regularizer_workspace_size": (c_size_t, [c_int]),
+    "uds_nearest_regularizer": (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_float, c_int, c_void_p, c_void_p,
+                                        c_void_p, c_void_p, c_size_t, c_void_p]),
     "uds_image_loss": (c_int, [c_int, c_size_t, c_void_p, c_void_p, c_float, c_void_p, c_void_p, c_void_p]),
     "uds_adam_splats": (c_int, [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p,
                                 c_void_p, c_void_p, c_void_p, c_int, c_float, c_float, c_float, c_float, c_float,

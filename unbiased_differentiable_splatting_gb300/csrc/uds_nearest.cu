@@ -126,3 +126,120 @@ extern "C" int uds_nearest_samples(int B, int W, int H, int K, const int32_t* in
     k_nearest_select<<<cdiv(N, 128), 128, 0, s>>>(N, num_nearest, points, offs, cand, nearest);
     return launch_status(6);
 }
+
+namespace uds {
+
+// ------------------------------------------------ nearest-sample regulariser
+// The two losses of NearestSamplesRegularizer (splatting/regularizier.py:
+// 119-175) over the nearest lists, with their gradients, in one pass: one
+// thread per splat i walks its M neighbours j (index > 0: the reference's
+// mask also drops index 0) and accumulates
+//   w_j = exp(-|n_i - n_j|^2 / s^2) exp(-|p_i - p_j|^2 / s^2),
+//   A = sum w_j, F = sum w_j n_j, D = sum w_j (p_i - p_j).n_j;
+// then plane_i = (D / (A + 1e-4))^2 and normal_i = min(1, #neighbours)
+// |F / (|F| + 1e-4) - n_i|^2.  The weights, the neighbours and the filtered
+// normal are constants of the loss (computed without gradient in the
+// reference), so d plane_i / d p_i = 2 D F / (A + 1e-4)^2 and
+// d normal_i / d n_i = -2 min(1, #) (F / (|F| + 1e-4) - n_i); gradients of
+// the neighbours' points and normals are zero.  The per-splat losses are
+// summed per block in a fixed order (warp trees, then warps), and the block
+// sums by one thread in block order: the result does not depend on timing.
+constexpr int kRegThreads = 256;
+
+__global__ void __launch_bounds__(kRegThreads) k_nearest_regularizer(
+    int N, int M, const int* __restrict__ nearest, const float* __restrict__ pts, const float* __restrict__ nrm,
+    float inv_s2, float scale, float* __restrict__ gpts, float* __restrict__ gnrm, float2* __restrict__ part) {
+    __shared__ float2 red[kRegThreads / 32];
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float normal_loss = 0.0f, plane_loss = 0.0f;
+    if (i < N) {
+        float p[3] = {pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]};
+        float n[3] = {nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]};
+        float A = 0.0f, D = 0.0f, F[3] = {0.0f, 0.0f, 0.0f};
+        int cnt = 0;
+        for (int m = 0; m < M; ++m) {
+            int j = nearest[(size_t)i * M + m];
+            if (j <= 0 || j >= N) continue;
+            ++cnt;
+            float q[3] = {pts[3 * j], pts[3 * j + 1], pts[3 * j + 2]};
+            float nj[3] = {nrm[3 * j], nrm[3 * j + 1], nrm[3 * j + 2]};
+            float dn2 = 0.0f, dp2 = 0.0f, pd = 0.0f;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                float a = n[c] - nj[c], b = p[c] - q[c];
+                dn2 += a * a;
+                dp2 += b * b;
+                pd += b * nj[c];
+            }
+            float w = expf(-dn2 * inv_s2) * expf(-dp2 * inv_s2);
+            A += w;
+            D += w * pd;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) F[c] += w * nj[c];
+        }
+        float inv = 1.0f / (A + 1e-4f);
+        float x = D * inv;
+        plane_loss = x * x;
+        float fn = 1.0f / (sqrtf(F[0] * F[0] + F[1] * F[1] + F[2] * F[2]) + 1e-4f);
+        float mask = cnt > 0 ? 1.0f : 0.0f;
+        float gp = scale * 2.0f * x * inv;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            float e = F[c] * fn - n[c];
+            normal_loss += e * e;
+            gnrm[3 * (size_t)i + c] = -scale * 2.0f * mask * e;
+            gpts[3 * (size_t)i + c] = gp * F[c];
+        }
+        normal_loss *= mask;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        normal_loss += __shfl_xor_sync(0xffffffffu, normal_loss, o);
+        plane_loss += __shfl_xor_sync(0xffffffffu, plane_loss, o);
+    }
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = make_float2(normal_loss, plane_loss);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float2 s = make_float2(0.0f, 0.0f);
+        for (int w = 0; w < kRegThreads / 32; ++w) {
+            s.x += red[w].x;
+            s.y += red[w].y;
+        }
+        part[blockIdx.x] = s;
+    }
+}
+
+__global__ void k_nearest_regularizer_sum(int nb, const float2* __restrict__ part, float scale,
+                                          float* __restrict__ losses) {
+    float2 s = make_float2(0.0f, 0.0f);
+    for (int b = 0; b < nb; ++b) {
+        s.x += part[b].x;
+        s.y += part[b].y;
+    }
+    losses[0] = s.x * scale;
+    losses[1] = s.y * scale;
+}
+
+}  // namespace uds
+
+extern "C" size_t uds_nearest_regularizer_workspace_size(int N) {
+    if (N < 0) return 0;
+    return sizeof(float2) * (size_t)cdiv(N > 0 ? N : 1, kRegThreads);
+}
+
+extern "C" int uds_nearest_regularizer(int N, int M, const int32_t* nearest, const float* points,
+                                       const float* normals, float sigma, int mean, float* losses,
+                                       float* grad_points, float* grad_normals, void* workspace,
+                                       size_t workspace_bytes, void* stream) {
+    if (N < 0 || M < 1 || !(sigma > 0.0f) || !losses || (N > 0 && (!nearest || !points || !normals ||
+                                                                   !grad_points || !grad_normals)))
+        return UDS_ERR_ARGUMENT;
+    if (!workspace || workspace_bytes < uds_nearest_regularizer_workspace_size(N)) return UDS_ERR_WORKSPACE;
+    cudaStream_t s = as_stream(stream);
+    int nb = (int)cdiv(N > 0 ? N : 1, kRegThreads);
+    float scale = (mean && N > 0) ? 1.0f / (float)N : 1.0f;
+    float2* part = reinterpret_cast<float2*>(workspace);
+    k_nearest_regularizer<<<nb, kRegThreads, 0, s>>>(N, M, nearest, points, normals, 1.0f / (sigma * sigma), scale,
+                                                      grad_points, grad_normals, part);
+    k_nearest_regularizer_sum<<<1, 1, 0, s>>>(nb, part, mean ? 1.0f / (float)(N > 0 ? N : 1) : 1.0f, losses);
+    return launch_status(2);
+}

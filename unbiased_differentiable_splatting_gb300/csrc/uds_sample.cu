@@ -902,6 +902,10 @@ __device__ float node_weight(const Tree& T, int v, float qx, float qy) {
     return w;
 }
 
+__device__ __noinline__ float node_weight_out_of_line(Tree T, int v, float qx, float qy) {
+    return node_weight(T, v, qx, qy);
+}
+
 // --------------------------------------------------------------- 8 sampler
 // Per-pixel mass cache.  getWeight(v) of a node without expansion that the
 // truncation circle reaches is the running sum, in depth-first order, of the
@@ -951,11 +955,16 @@ struct MassCache {
 // acc[depth][lane]: every lane inside a node has opened the same ancestors,
 // so the update loop over them has one trip count per warp and touches one
 // bank per lane; each sum is written to the lane's cache once, when its node
-// is closed.
+// is closed.  The stack holds kWalkDepth levels (the trees built here are
+// about 20-30 deep; a smaller block leaves more of the SM's L1 to the
+// per-lane caches).  A lane whose walk would go deeper gives up its cache
+// (the descent then evaluates masses directly) and takes its total from a
+// direct subtree walk.
+constexpr int kWalkDepth = 40;
 struct WalkStack {
-    unsigned mask[kTrace];  // lanes that opened the ancestor at this depth
-    int right[kTrace];      // its right child
-    float acc[kTrace][32];
+    unsigned mask[kWalkDepth];  // lanes that opened the ancestor at this depth
+    int right[kWalkDepth];      // its right child
+    float acc[kWalkDepth][32];
 };
 
 __device__ void warp_root_walk(const Tree& T, float qx, float qy, bool live, MassCache& mc, float& total,
@@ -974,15 +983,16 @@ __device__ void warp_root_walk(const Tree& T, float qx, float qy, bool live, Mas
     if (!liveMask) return;
     // per opened ancestor (same index in every lane inside): its entry, its
     // left child's entry and where its right child's entry would start
-    int ostack[kTrace], lstack[kTrace], rstack[kTrace];
+    int ostack[kWalkDepth], lstack[kWalkDepth], rstack[kWalkDepth];
     int osp = 0;
     int sp = -1;                    // deepest opened ancestor of v
     unsigned long long onright = 0; // bit k: ancestor k's right subtree is under way
     int v = 0;                      // node entered next, and the lanes inside it
     unsigned in = liveMask;
+    bool deep = false;  // a subtree was not walked: total is incomplete
     int budget = 4 * T.n + 64;
     while (true) {
-        if (--budget < 0) { mc.ok = false; break; }
+        if (--budget < 0) { mc.ok = false; deep = true; break; }
         bool mine = (in >> lane) & 1u;
         c = T.cen[v];
         float4 bx = T.box[v];
@@ -1006,11 +1016,14 @@ __device__ void warp_root_walk(const Tree& T, float qx, float qy, bool live, Mas
             bool op = mine && !truncated_box(bx, c.z, qx, qy);
             unsigned opened = __ballot_sync(full, op);
             // v sits at depth sp + 1; its children would be at sp + 2
-            if (opened && sp + 2 >= kTrace) {
-                mc.ok = false;  // deeper than any tree built here
+            if (opened && sp + 2 >= kWalkDepth) {
+                if (op) {  // this lane's subtree below v is not walked
+                    mc.ok = false;
+                    deep = true;
+                }
             } else if (opened) {
                 if (op && mc.ok) {
-                    if (mc.m < kTable && osp < kTrace) {
+                    if (mc.m < kTable && osp < kWalkDepth) {
                         ws.acc[osp][lane] = 0.0f;
                         ostack[osp++] = mc.m++;
                     } else {
@@ -1059,6 +1072,9 @@ __device__ void warp_root_walk(const Tree& T, float qx, float qy, bool live, Mas
         if (!more) break;
         __syncwarp();  // the stack slots read above may be rewritten next
     }
+    // the same running sum in the same order, by a direct walk (rare: out of
+    // line)
+    if (deep && live) total = node_weight_out_of_line(T, 0, qx, qy);
 }
 
 template <int R, int KM>

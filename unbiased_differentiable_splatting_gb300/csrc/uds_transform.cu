@@ -144,9 +144,86 @@ __global__ void k_view_matrix_backward(int B, const float* __restrict__ G, const
     for (int k = 0; k < 4; ++k) gquat[4 * b + k] = gq[k];
 }
 
+// BackfaceCulling (render.py:193-205): a splat whose camera-space normal
+// points away from the camera (z > 0) gets its camera-space normal and, when
+// given, its world normal negated; everything else is copied.  One thread per
+// (view, splat); world normals (nB,N,3) with nB in {1, B}.
+__global__ void k_backface_forward(int B, int N, const float* __restrict__ cam, int nB,
+                                   const float* __restrict__ world, float* __restrict__ out_cam,
+                                   float* __restrict__ out_world) {
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    int b = blockIdx.y;
+    if (x >= N) return;
+    size_t o = 3 * ((size_t)x + (size_t)N * b);
+    float c0 = cam[o], c1 = cam[o + 1], c2 = cam[o + 2];
+    bool flip = c2 > 0.0f;
+    out_cam[o] = flip ? -c0 : c0;
+    out_cam[o + 1] = flip ? -c1 : c1;
+    out_cam[o + 2] = flip ? -c2 : c2;
+    if (world) {
+        const float* w = world + 3 * ((size_t)x + (nB > 1 ? (size_t)N * b : 0));
+#pragma unroll
+        for (int k = 0; k < 3; ++k) out_world[o + k] = flip ? -w[k] : w[k];
+    }
+}
+
+// Gradients of the flips: the camera-space one per (view, splat); the world
+// one summed over the views in view order when the normals are shared.
+__global__ void k_backface_backward(int B, int N, const float* __restrict__ cam, const float* __restrict__ g_cam,
+                                    int nB, const float* __restrict__ g_world, float* __restrict__ gcam_out,
+                                    float* __restrict__ gworld_out) {
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= N) return;
+    float acc[3] = {0.0f, 0.0f, 0.0f};
+    for (int b = 0; b < B; ++b) {
+        size_t o = 3 * ((size_t)x + (size_t)N * b);
+        float sgn = cam[o + 2] > 0.0f ? -1.0f : 1.0f;
+        if (g_cam) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) gcam_out[o + k] = sgn * g_cam[o + k];
+        }
+        if (g_world) {
+            if (nB > 1) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) gworld_out[o + k] = sgn * g_world[o + k];
+            } else {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) acc[k] += sgn * g_world[o + k];
+            }
+        }
+    }
+    if (g_world && nB == 1) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) gworld_out[3 * (size_t)x + k] = acc[k];
+    }
+}
+
 }  // namespace uds
 
 using namespace uds;
+
+extern "C" int uds_backface_forward(int B, int N, const float* cam_normals, int nB, const float* normals,
+                                    float* flipped_cam, float* flipped_normals, void* stream) {
+    if (B <= 0 || N < 0 || (normals && nB != 1 && nB != B) || (N > 0 && (!cam_normals || !flipped_cam)) ||
+        (normals && !flipped_normals))
+        return UDS_ERR_ARGUMENT;
+    if (N == 0) return UDS_OK;
+    k_backface_forward<<<dim3(cdiv(N, 256), B), 256, 0, as_stream(stream)>>>(B, N, cam_normals, nB, normals,
+                                                                             flipped_cam, flipped_normals);
+    return launch_status();
+}
+
+extern "C" int uds_backface_backward(int B, int N, const float* cam_normals, const float* grad_flipped_cam, int nB,
+                                     const float* grad_flipped_normals, float* grad_cam, float* grad_normals,
+                                     void* stream) {
+    if (B <= 0 || N < 0 || (grad_flipped_normals && nB != 1 && nB != B) || (N > 0 && !cam_normals) ||
+        (grad_flipped_cam && !grad_cam) || (grad_flipped_normals && !grad_normals))
+        return UDS_ERR_ARGUMENT;
+    if (N == 0) return UDS_OK;
+    k_backface_backward<<<cdiv(N, 256), 256, 0, as_stream(stream)>>>(B, N, cam_normals, grad_flipped_cam, nB,
+                                                                     grad_flipped_normals, grad_cam, grad_normals);
+    return launch_status();
+}
 
 extern "C" int uds_transform_forward(int affine, int B, const float* M, int vB, int N,
                                      const float* v, float* out, void* stream) {

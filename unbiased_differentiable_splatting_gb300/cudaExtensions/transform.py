@@ -1,5 +1,6 @@
-"""cudaExtensions.transform (transform.cpp:33-86), and the view matrix of
-world2Camera (utils.py:11-49)."""
+"""cudaExtensions.transform (transform.cpp:33-86), the view matrix of
+world2Camera (utils.py:11-49) and the normal flips of BackfaceCulling
+(render.py:193-205)."""
 from __future__ import annotations
 
 import torch
@@ -70,3 +71,41 @@ def viewMatrixBackward(gradIn: torch.Tensor, quaternions: torch.Tensor):
     check(load().uds_view_matrix_backward(B, ptr(gradIn), ptr(quaternions), ptr(gp), ptr(gq),
                                           stream_ptr(gradIn.device)), "view matrix backward")
     return gp, gq
+
+
+def backfaceForward(camNormals: torch.Tensor, normals=None):
+    """(B,N,3) camera-space normals, optional (1|B,N,3) world normals ->
+    [flipped camera-space normals (B,N,3)] + [flipped world normals (B,N,3)]
+    when normals is given."""
+    need(camNormals, "camNormals")
+    if camNormals.dim() != 3 or camNormals.shape[2] != 3:
+        raise ValueError("camNormals must be (B,N,3)")
+    B, N = camNormals.shape[0], camNormals.shape[1]
+    fc = torch.empty_like(camNormals)
+    fw = None
+    if normals is not None:
+        need(normals, "normals", device=camNormals.device)
+        if normals.dim() != 3 or normals.shape[1:] != camNormals.shape[1:] or normals.shape[0] not in (1, B):
+            raise ValueError("normals must be (1|B,N,3)")
+        fw = torch.empty_like(camNormals)
+    check(load().uds_backface_forward(B, N, ptr(camNormals), normals.shape[0] if normals is not None else 1,
+                                      ptr(normals), ptr(fc), ptr(fw), stream_ptr(camNormals.device)),
+          "backface forward")
+    return [fc] if fw is None else [fc, fw]
+
+
+def backfaceBackward(camNormals: torch.Tensor, gradCam=None, gradNormals=None, normalsBatch: int = 1):
+    """Gradients of backfaceForward: [grad camNormals or None, grad normals
+    (normalsBatch,N,3) or None]."""
+    need(camNormals, "camNormals")
+    B, N = camNormals.shape[0], camNormals.shape[1]
+    gc = gw = None
+    if gradCam is not None:
+        need(gradCam, "gradCam", device=camNormals.device)
+        gc = torch.empty_like(camNormals)
+    if gradNormals is not None:
+        need(gradNormals, "gradNormals", device=camNormals.device)
+        gw = torch.empty((normalsBatch, N, 3), dtype=torch.float32, device=camNormals.device)
+    check(load().uds_backface_backward(B, N, ptr(camNormals), ptr(gradCam), normalsBatch, ptr(gradNormals), ptr(gc),
+                                       ptr(gw), stream_ptr(camNormals.device)), "backface backward")
+    return gc, gw

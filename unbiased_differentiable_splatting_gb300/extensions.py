@@ -2,6 +2,9 @@
 and gradient conventions of the reference's ``splatting/extensions/__init__.py``
 (lines 104-581) and the helpers of ``splatting/extensions/utils.py``.
 
+Every class calls the ops registered in ``library`` (``torch.ops.uds.*``), so
+the dispatcher, fake tensors and ``torch.compile`` see them.
+
 Gradient conventions kept from the reference:
 * ``EWASplatting.backward`` clamps each splat's point / std-dev gradient to
   norm <= 1 (``conditionalNormalization``), zeroes NaNs and returns no gradient
@@ -13,7 +16,10 @@ from __future__ import annotations
 
 import torch as th
 
-from .cudaExtensions import filtering, interpolation, pixelgather, sampling, shading, splatting, transform
+from . import library  # noqa: F401  (registers torch.ops.uds)
+from .cudaExtensions import sampling
+
+ops = th.ops.uds
 
 
 # ------------------------------------------------------------------ utils
@@ -36,12 +42,12 @@ class ViewMatrix(th.autograd.Function):
         q = camQuaternion.contiguous()
         ctx.save_for_backward(q)
         ctx.pshape = camPositions.shape
-        return transform.viewMatrixForward(camPositions.reshape(-1, 3).contiguous(), q)
+        return ops.view_matrix_forward(camPositions.reshape(-1, 3).contiguous(), q)
 
     @staticmethod
     def backward(ctx, gradIn):
         (q,) = ctx.saved_tensors
-        gp, gq = transform.viewMatrixBackward(gradIn.contiguous(), q)
+        gp, gq = ops.view_matrix_backward(gradIn.contiguous(), q)
         return gp.reshape(ctx.pshape), gq
 
 
@@ -87,12 +93,26 @@ def conditionalNormalization(dx: th.Tensor, radius=1.0, eps=1e-4) -> th.Tensor:
 
 # --------------------------------------------------------------- sampling
 class FmmSampling:
-    """extensions/__init__.py:106-117"""
+    """extensions/__init__.py:106-117.  Calls ``torch.ops.uds.sample`` when the
+    keyword arguments are at most ``seed`` and ``uniforms``; the additions the
+    op schema leaves out (``h``, ``return_stats``, ``tile_x``, ...) go to
+    ``cudaExtensions.sampling.sample`` directly."""
 
     @th.no_grad()
     def __call__(self, width: int, height: int, focallength: float, points: th.Tensor, normals: th.Tensor,
                  colors: th.Tensor, stdDevs: th.Tensor, numSamples: int, smoothing: float,
                  precision: float = 0.001, **kwargs) -> th.Tensor:
+        if set(kwargs) <= {"seed", "uniforms"}:
+            seed = kwargs.get("seed")
+            if seed is None:
+                seed = int(th.randint(0, 2 ** 62, (1,)).item())
+            tensor_seed = isinstance(seed, th.Tensor)
+            if not tensor_seed:  # the 64-bit Philox key as the schema's signed int64
+                seed = int(seed) & 0xFFFFFFFFFFFFFFFF
+                seed = seed - (1 << 64) if seed >= (1 << 63) else seed
+            return ops.sample(int(width), int(height), float(focallength), points, normals, stdDevs, int(numSamples),
+                              float(smoothing), float(precision), 0 if tensor_seed else int(seed),
+                              seed if tensor_seed else None, kwargs.get("uniforms"))
         return sampling.sample(width, height, focallength, points, normals, colors, stdDevs, numSamples, smoothing,
                                precision, **kwargs)
 
@@ -102,12 +122,12 @@ class AffineTransform(th.autograd.Function):
     @staticmethod
     def forward(ctx, transformMatrix, vector):
         ctx.save_for_backward(transformMatrix, vector)
-        return transform.affineForward(transformMatrix.contiguous(), vector.contiguous())
+        return ops.affine_forward(transformMatrix.contiguous(), vector.contiguous())
 
     @staticmethod
     def backward(ctx, gradIn):
         M, v = ctx.saved_tensors
-        gM, gv = transform.affineBackward(gradIn.contiguous(), M.contiguous(), v.contiguous())
+        gM, gv = ops.affine_backward(gradIn.contiguous(), M.contiguous(), v.contiguous())
         return gM, gv
 
 
@@ -115,12 +135,12 @@ class LinearTransform(th.autograd.Function):
     @staticmethod
     def forward(ctx, transformMatrix, vector):
         ctx.save_for_backward(transformMatrix, vector)
-        return transform.linearForward(transformMatrix.contiguous(), vector.contiguous())
+        return ops.linear_forward(transformMatrix.contiguous(), vector.contiguous())
 
     @staticmethod
     def backward(ctx, gradIn):
         M, v = ctx.saved_tensors
-        gM, gv = transform.linearBackward(gradIn.contiguous(), M.contiguous(), v.contiguous())
+        gM, gv = ops.linear_backward(gradIn.contiguous(), M.contiguous(), v.contiguous())
         return gM, gv
 
 
@@ -130,7 +150,8 @@ class EWASplatting(th.autograd.Function):
     def forward(ctx, width: int, height: int, focallength: float, indices: th.Tensor, points: th.Tensor,
                 normals: th.Tensor, stdDevs: th.Tensor, smoothing: float) -> th.Tensor:
         points, normals, stdDevs = points.contiguous(), normals.contiguous(), stdDevs.contiguous()
-        weights = splatting.forward(width, height, focallength, indices, points, normals, stdDevs, smoothing)
+        weights = ops.splat_forward(width, height, float(focallength), indices, points, normals, stdDevs,
+                                    float(smoothing))
         ctx.save_for_backward(indices, points, normals, stdDevs)
         ctx.width, ctx.height, ctx.focallength, ctx.smoothing = width, height, focallength, smoothing
         return weights
@@ -138,9 +159,9 @@ class EWASplatting(th.autograd.Function):
     @staticmethod
     def backward(ctx, gradWeights):
         indices, points, normals, stdDevs = ctx.saved_tensors
-        gradPoints, gradNormals, gradStdDevs = splatting.backward(ctx.width, ctx.height, ctx.focallength,
+        gradPoints, gradNormals, gradStdDevs = ops.splat_backward(ctx.width, ctx.height, float(ctx.focallength),
                                                                   gradWeights.contiguous(), indices, points, normals,
-                                                                  stdDevs, ctx.smoothing)
+                                                                  stdDevs, float(ctx.smoothing))
         gradPoints = conditionalNormalization(gradPoints)
         gradStdDevs = conditionalNormalization(gradStdDevs)
         gradPoints = th.nan_to_num(gradPoints, nan=0.0, posinf=float("inf"), neginf=float("-inf"))
@@ -155,13 +176,13 @@ class DepthFiltering(th.autograd.Function):
         weights, points, normals = weights.contiguous(), points.contiguous(), normals.contiguous()
         ctx.save_for_backward(indices, weights, points, normals)
         ctx.width, ctx.height, ctx.focallength = width, height, focallength
-        return filtering.forward(indices, weights, width, height, focallength, points, normals)
+        return ops.filter_forward(indices, weights, width, height, float(focallength), points, normals)
 
     @staticmethod
     def backward(ctx, gradIn):
         indices, weights, points, normals = ctx.saved_tensors
-        gradWeights = filtering.backward(indices, weights, gradIn.contiguous(), ctx.width, ctx.height,
-                                         ctx.focallength, points, normals)
+        gradWeights = ops.filter_backward(indices, weights, gradIn.contiguous(), ctx.width, ctx.height,
+                                          float(ctx.focallength), points, normals)
         return None, gradWeights, None, None, None, None, None
 
 
@@ -171,12 +192,12 @@ class LinearInterpolation(th.autograd.Function):
     def forward(ctx, indices, weights, values):
         weights, values = weights.contiguous(), values.contiguous()
         ctx.save_for_backward(indices, weights, values)
-        return interpolation.forward(indices, weights, values)
+        return ops.interp_forward(indices, weights, values)
 
     @staticmethod
     def backward(ctx, gradIn):
         indices, weights, values = ctx.saved_tensors
-        gradWeights, gradValues = interpolation.backward(gradIn.contiguous(), indices, weights, values)
+        gradWeights, gradValues = ops.interp_backward(gradIn.contiguous(), indices, weights, values)
         return None, gradWeights, gradValues
 
 
@@ -187,12 +208,12 @@ class DiffuseShading(th.autograd.Function):
         directions, intensites = directions.contiguous(), intensites.contiguous()
         normals, diffuse = normals.contiguous(), diffuse.contiguous()
         ctx.save_for_backward(directions, intensites, normals, diffuse)
-        return shading.forward(directions, intensites, normals, diffuse)
+        return ops.shade_forward(directions, intensites, normals, diffuse)
 
     @staticmethod
     def backward(ctx, gradIn):
         directions, intensites, normals, diffuse = ctx.saved_tensors
-        return tuple(shading.backward(gradIn.contiguous(), directions, intensites, normals, diffuse))
+        return tuple(ops.shade_backward(gradIn.contiguous(), directions, intensites, normals, diffuse))
 
 
 class LambertShading(th.autograd.Function):
@@ -203,11 +224,11 @@ class LambertShading(th.autograd.Function):
     def forward(ctx, ambient, directions, intensities, normals, diffuse):
         ts = [t.contiguous() for t in (ambient, directions, intensities, normals, diffuse)]
         ctx.save_for_backward(*ts)
-        return shading.lambertForward(*ts)
+        return ops.lambert_forward(*ts)
 
     @staticmethod
     def backward(ctx, gradIn):
-        return tuple(shading.lambertBackward(gradIn.contiguous(), *ctx.saved_tensors))
+        return tuple(ops.lambert_backward(gradIn.contiguous(), *ctx.saved_tensors))
 
 
 class SphericalHarmonicShading(th.autograd.Function):
@@ -215,12 +236,12 @@ class SphericalHarmonicShading(th.autograd.Function):
     def forward(ctx, coefficients, normals, diffuse):
         coefficients, normals, diffuse = coefficients.contiguous(), normals.contiguous(), diffuse.contiguous()
         ctx.save_for_backward(coefficients, normals, diffuse)
-        return shading.forwardSh(coefficients, normals, diffuse)
+        return ops.shade_sh_forward(coefficients, normals, diffuse)
 
     @staticmethod
     def backward(ctx, gradIn):
         coefficients, normals, diffuse = ctx.saved_tensors
-        return tuple(shading.backwardSh(gradIn.contiguous(), coefficients, normals, diffuse))
+        return tuple(ops.shade_sh_backward(gradIn.contiguous(), coefficients, normals, diffuse))
 
 
 __all__ = ["FmmSampling", "AffineTransform", "LinearTransform", "EWASplatting", "DepthFiltering",
@@ -239,9 +260,9 @@ class PixelScatterGather(th.autograd.Function):
     def forward(ctx, indices, values):
         ctx.save_for_backward(indices)
         ctx.numSources = values.shape[1]
-        return pixelgather.scatter(indices, values.contiguous())
+        return ops.pixel_scatter(indices, values.contiguous())
 
     @staticmethod
     def backward(ctx, grad_output):
         (indices,) = ctx.saved_tensors
-        return None, pixelgather.gather(indices, grad_output.contiguous(), ctx.numSources)
+        return None, ops.pixel_gather(indices, grad_output.contiguous(), ctx.numSources, False)

@@ -1,26 +1,44 @@
-"""Nearest-sample regulariser (splatting/regularizier.py:119-175), on top of
-``cudaExtensions.nearestsamples.nearest``.
+"""Nearest-sample regulariser with the interface of the reference's
+``NearestSamplesRegularizer`` (splatting/regularizier.py:119-175).
 
-For every splat the neighbours come from the pixels where it is the surface
-sample; the regulariser pulls each splat towards the planes of its
-neighbours (plane loss) and its normal towards their weighted mean normal
-(normal loss), with Gaussian weights on point and normal distances.  The
-formula is the reference's, including its mask ``nearest > 0`` (which also
-drops neighbour index 0).
+For every splat the neighbours are the splats sampled together with it in
+the pixels where it is the surface sample (``nearestsamples.nearest``).  Two
+losses pull the surface together: the plane loss, the squared weighted mean
+distance of the splat from its neighbours' tangent planes, and the normal
+loss, the squared distance of the splat's normal from its neighbours'
+weighted mean normal; neighbour weights are Gaussians of the point and normal
+distances with width ``sigma``.  Both losses and their gradients come from
+one CUDA kernel over the neighbour lists (``nearestsamples.regularizer``);
+as in the reference, the weights, the neighbours and the mean normals are
+constants of the loss, and neighbour index 0 is masked.
 """
 from __future__ import annotations
 
 import torch as th
 
 from .cudaExtensions import nearestsamples
-from .extensions import normalize
+
+REDUCTIONS = ("sum", "mean")
 
 
-def _dot(a, b):
-    return th.sum(a * b, dim=-1, keepdim=True)
+class _NearestLosses(th.autograd.Function):
+    @staticmethod
+    def forward(ctx, points, normals, nearest, sigma, mean):
+        losses, gp, gn = nearestsamples.regularizer(nearest, points.detach().contiguous(),
+                                                    normals.detach().contiguous(), sigma, mean)
+        ctx.save_for_backward(gp, gn)
+        return losses[0], losses[1]
+
+    @staticmethod
+    def backward(ctx, g_normal, g_plane):
+        gp, gn = ctx.saved_tensors
+        return gp * g_plane, gn * g_normal, None, None, None
 
 
 class NearestSamplesRegularizer(th.nn.Module):
+    """forward(indices, weights, points, normals) -> (normal loss, plane loss),
+    summed over splats ("sum") or averaged ("mean")."""
+
     def __init__(self, sigma=0.5, num_nearest=10, reduction="sum") -> None:
         super().__init__()
         self.sigma = sigma
@@ -28,29 +46,10 @@ class NearestSamplesRegularizer(th.nn.Module):
         self.reduction = reduction
         self.nearest = nearestsamples.nearest
 
-    def _gaussian(self, x):
-        return th.exp(-x.square() / self.sigma ** 2)
-
     def forward(self, indices, weights, points, normals):
+        if self.reduction not in REDUCTIONS:
+            raise ValueError(f"unknown reduction mode {self.reduction!r}")
         with th.no_grad():
-            nearestIndices = self.nearest(indices, weights.contiguous(), points.detach().contiguous(),
-                                          self.num_nearest)
-            mask = (nearestIndices > 0).to(points.dtype).unsqueeze(-1)
-            nearestIndices = nearestIndices.clamp(0)
-            nearestPoints = points[0, nearestIndices[0].long(), :].unsqueeze(0)
-            nearestNormals = normals[0, nearestIndices[0].long(), :].unsqueeze(0)
-            anisotropic = (normals.unsqueeze(2) - nearestNormals).norm(dim=-1, keepdim=True)
-            isotropic = (points.unsqueeze(2) - nearestPoints.detach()).norm(dim=-1, keepdim=True)
-            w = mask * self._gaussian(anisotropic) * self._gaussian(isotropic)
-            invWeights = 1.0 / (w.sum(dim=2) + 1e-4)
-            filteredNormals = normalize(th.sum(w * nearestNormals, dim=2))
-            pixelMask = mask.sum(dim=2).clamp(0, 1)
-        planeDistance = w.detach() * _dot(points.unsqueeze(2) - nearestPoints.detach(), nearestNormals.detach())
-        planeLoss = th.square(invWeights.detach() * planeDistance.sum(dim=2))
-        normalDistance = th.square(filteredNormals.detach() - normals).sum(dim=-1, keepdim=True)
-        normalLoss = pixelMask.detach() * normalDistance
-        if self.reduction == "sum":
-            return normalLoss.sum(), planeLoss.sum()
-        if self.reduction == "mean":
-            return normalLoss.mean(), planeLoss.mean()
-        raise ValueError("Unkown reduction mode")
+            nearest = self.nearest(indices, weights.detach().contiguous(), points.detach().contiguous(),
+                                   self.num_nearest)
+        return _NearestLosses.apply(points, normals, nearest, float(self.sigma), self.reduction == "mean")

@@ -41,14 +41,14 @@ def _cosine(normal: th.Tensor, light: th.Tensor) -> th.Tensor:
 
 
 class BackfaceCulling(th.nn.Module):
-    """render.py:193-205: flip normals that face away from the camera.  With
-    ``normals`` None only the camera-space normals are flipped (the shading
-    modes that do not read the flipped world normals)."""
+    """render.py:193-205: flip normals that face away from the camera, in one
+    kernel (``torch.ops.uds.backface``, differentiable).  With ``normals``
+    None only the camera-space normals are flipped (the shading modes that do
+    not read the flipped world normals)."""
 
     def forward(self, normals, camNormals):
-        facing = camNormals[..., 2].unsqueeze(-1) > 0
-        flipped = None if normals is None else th.where(facing, -normals, normals)
-        return flipped, th.where(facing, -camNormals, camNormals)
+        out = th.ops.uds.backface(camNormals.contiguous(), None if normals is None else normals.contiguous())
+        return (None if normals is None else out[1]), out[0]
 
 
 class Lambert(th.nn.Module):
