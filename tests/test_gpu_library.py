@@ -43,6 +43,7 @@ def test_opcheck_sampler_and_render_chain(ops):
     assert (idx >= 0).any()
     p, n, s = (x.clone().requires_grad_(True) for x in (pts, nrm, sd))
     _check(ops.splat_forward.default, (W, H, f, idx, p, n, s, 0.0))
+    _check(ops.ewa_weights.default, (W, H, f, idx, p, n, s, 0.0))
     w = ops.splat_forward(W, H, f, idx, pts, nrm, sd, 0.0)
     _check(ops.splat_backward.default, (W, H, f, torch.ones_like(w), idx, pts, nrm, sd, 0.0))
     _check(ops.filter_forward.default, (idx, w.clone().requires_grad_(True), W, H, f, pts, nrm))

@@ -2,8 +2,10 @@
 and gradient conventions of the reference's ``splatting/extensions/__init__.py``
 (lines 104-581) and the helpers of ``splatting/extensions/utils.py``.
 
-Every class calls the ops registered in ``library`` (``torch.ops.uds.*``), so
-the dispatcher, fake tensors and ``torch.compile`` see them.
+Every class is a thin callable over the ops registered in ``library``
+(``torch.ops.uds.*``, whose autograd formulas are registered with the
+dispatcher), so fake tensors and ``torch.compile`` see them; ``X.apply(...)``
+takes the reference's arguments.
 
 Gradient conventions kept from the reference:
 * ``EWASplatting.backward`` clamps each splat's point / std-dev gradient to
@@ -33,24 +35,6 @@ def dot(x: th.Tensor, y: th.Tensor, keepdim: bool) -> th.Tensor:
     return th.sum(x.mul(y), dim=-1, keepdim=keepdim)
 
 
-class ViewMatrix(th.autograd.Function):
-    """world2Camera on the GPU: one kernel each way (the forward rounds like
-    the reference's tensor operations, so the matrix is the same)."""
-
-    @staticmethod
-    def forward(ctx, camPositions, camQuaternion):
-        q = camQuaternion.contiguous()
-        ctx.save_for_backward(q)
-        ctx.pshape = camPositions.shape
-        return ops.view_matrix_forward(camPositions.reshape(-1, 3).contiguous(), q)
-
-    @staticmethod
-    def backward(ctx, gradIn):
-        (q,) = ctx.saved_tensors
-        gp, gq = ops.view_matrix_backward(gradIn.contiguous(), q)
-        return gp.reshape(ctx.pshape), gq
-
-
 def world2Camera(camPositions: th.Tensor, camQuaternion: th.Tensor) -> th.Tensor:
     """Quaternion (x, y, z, w) + translation -> (B,1,4,4) view matrix
     (Euler-Rodrigues rotation, utils.py:11-49): the fused kernels for float32
@@ -60,7 +44,7 @@ def world2Camera(camPositions: th.Tensor, camQuaternion: th.Tensor) -> th.Tensor
             and camQuaternion.dtype == th.float32 and camPositions.device == camQuaternion.device
             and camQuaternion.dim() == 2 and camQuaternion.shape[1] == 4 and camPositions.numel() == 3 * B
             and camQuaternion.shape[0] == B):
-        return ViewMatrix.apply(camPositions, camQuaternion)
+        return ops.view_matrix_forward(camPositions.reshape(B, 3).contiguous(), camQuaternion.contiguous())
     x, y, z, w = camQuaternion.split(1, dim=-1)
     x2, y2, z2, w2 = x * x, y * y, z * z, w * w
     xy, zw, xz, yw, yz, xw = x * y, z * w, x * z, y * w, y * z, x * w
@@ -117,131 +101,76 @@ class FmmSampling:
                                precision, **kwargs)
 
 
+class _OpFunction:
+    """A reference autograd-Function name over a registered op: ``apply``
+    takes the reference's arguments, makes the tensors contiguous and calls
+    the op, whose autograd formula is registered with the dispatcher (so
+    torch.compile traces it without an autograd.Function)."""
+
+    op_name = ""
+
+    @classmethod
+    def apply(cls, *args):
+        args = [a.contiguous() if isinstance(a, th.Tensor) else a for a in args]
+        return getattr(ops, cls.op_name)(*args)
+
+
 # --------------------------------------------------------------- transform
-class AffineTransform(th.autograd.Function):
-    @staticmethod
-    def forward(ctx, transformMatrix, vector):
-        ctx.save_for_backward(transformMatrix, vector)
-        return ops.affine_forward(transformMatrix.contiguous(), vector.contiguous())
-
-    @staticmethod
-    def backward(ctx, gradIn):
-        M, v = ctx.saved_tensors
-        gM, gv = ops.affine_backward(gradIn.contiguous(), M.contiguous(), v.contiguous())
-        return gM, gv
+class AffineTransform(_OpFunction):
+    """AffineTransform.apply(M (B,4,4), v (1|B,N,3)) -> (B,N,3)."""
+    op_name = "affine_forward"
 
 
-class LinearTransform(th.autograd.Function):
-    @staticmethod
-    def forward(ctx, transformMatrix, vector):
-        ctx.save_for_backward(transformMatrix, vector)
-        return ops.linear_forward(transformMatrix.contiguous(), vector.contiguous())
-
-    @staticmethod
-    def backward(ctx, gradIn):
-        M, v = ctx.saved_tensors
-        gM, gv = ops.linear_backward(gradIn.contiguous(), M.contiguous(), v.contiguous())
-        return gM, gv
+class LinearTransform(_OpFunction):
+    """LinearTransform.apply(M (B,4,4), v (1|B,N,3)) -> (B,N,3)."""
+    op_name = "linear_forward"
 
 
 # ------------------------------------------------------------------- EWA
-class EWASplatting(th.autograd.Function):
-    @staticmethod
-    def forward(ctx, width: int, height: int, focallength: float, indices: th.Tensor, points: th.Tensor,
-                normals: th.Tensor, stdDevs: th.Tensor, smoothing: float) -> th.Tensor:
-        points, normals, stdDevs = points.contiguous(), normals.contiguous(), stdDevs.contiguous()
-        weights = ops.splat_forward(width, height, float(focallength), indices, points, normals, stdDevs,
-                                    float(smoothing))
-        ctx.save_for_backward(indices, points, normals, stdDevs)
-        ctx.width, ctx.height, ctx.focallength, ctx.smoothing = width, height, focallength, smoothing
-        return weights
+class EWASplatting(_OpFunction):
+    """EWASplatting.apply(width, height, focallength, indices, points,
+    normals, stdDevs, smoothing) -> weights (B,W,H,K); gradients with the
+    reference's post-processing (``torch.ops.uds.ewa_weights``)."""
 
-    @staticmethod
-    def backward(ctx, gradWeights):
-        indices, points, normals, stdDevs = ctx.saved_tensors
-        gradPoints, gradNormals, gradStdDevs = ops.splat_backward(ctx.width, ctx.height, float(ctx.focallength),
-                                                                  gradWeights.contiguous(), indices, points, normals,
-                                                                  stdDevs, float(ctx.smoothing))
-        gradPoints = conditionalNormalization(gradPoints)
-        gradStdDevs = conditionalNormalization(gradStdDevs)
-        gradPoints = th.nan_to_num(gradPoints, nan=0.0, posinf=float("inf"), neginf=float("-inf"))
-        gradStdDevs = th.nan_to_num(gradStdDevs, nan=0.0, posinf=float("inf"), neginf=float("-inf"))
-        return None, None, None, None, gradPoints, None, gradStdDevs, None
+    @classmethod
+    def apply(cls, width, height, focallength, indices, points, normals, stdDevs, smoothing):
+        return ops.ewa_weights(int(width), int(height), float(focallength), indices, points.contiguous(),
+                               normals.contiguous(), stdDevs.contiguous(), float(smoothing))
 
 
 # ------------------------------------------------------------ compositing
-class DepthFiltering(th.autograd.Function):
-    @staticmethod
-    def forward(ctx, indices, weights, width: int, height: int, focallength: float, points, normals):
-        weights, points, normals = weights.contiguous(), points.contiguous(), normals.contiguous()
-        ctx.save_for_backward(indices, weights, points, normals)
-        ctx.width, ctx.height, ctx.focallength = width, height, focallength
-        return ops.filter_forward(indices, weights, width, height, float(focallength), points, normals)
+class DepthFiltering(_OpFunction):
+    """DepthFiltering.apply(indices, weights, width, height, focallength,
+    points, normals) -> depth weights; gradients for the weights only."""
 
-    @staticmethod
-    def backward(ctx, gradIn):
-        indices, weights, points, normals = ctx.saved_tensors
-        gradWeights = ops.filter_backward(indices, weights, gradIn.contiguous(), ctx.width, ctx.height,
-                                          float(ctx.focallength), points, normals)
-        return None, gradWeights, None, None, None, None, None
+    @classmethod
+    def apply(cls, indices, weights, width, height, focallength, points, normals):
+        return ops.filter_forward(indices, weights.contiguous(), int(width), int(height), float(focallength),
+                                  points.contiguous(), normals.contiguous())
 
 
 # ---------------------------------------------------------- interpolation
-class LinearInterpolation(th.autograd.Function):
-    @staticmethod
-    def forward(ctx, indices, weights, values):
-        weights, values = weights.contiguous(), values.contiguous()
-        ctx.save_for_backward(indices, weights, values)
-        return ops.interp_forward(indices, weights, values)
-
-    @staticmethod
-    def backward(ctx, gradIn):
-        indices, weights, values = ctx.saved_tensors
-        gradWeights, gradValues = ops.interp_backward(gradIn.contiguous(), indices, weights, values)
-        return None, gradWeights, gradValues
+class LinearInterpolation(_OpFunction):
+    """LinearInterpolation.apply(indices, weights, values (1|B,N,C))."""
+    op_name = "interp_forward"
 
 
 # ---------------------------------------------------------------- shading
-class DiffuseShading(th.autograd.Function):
-    @staticmethod
-    def forward(ctx, directions, intensites, normals, diffuse):
-        directions, intensites = directions.contiguous(), intensites.contiguous()
-        normals, diffuse = normals.contiguous(), diffuse.contiguous()
-        ctx.save_for_backward(directions, intensites, normals, diffuse)
-        return ops.shade_forward(directions, intensites, normals, diffuse)
-
-    @staticmethod
-    def backward(ctx, gradIn):
-        directions, intensites, normals, diffuse = ctx.saved_tensors
-        return tuple(ops.shade_backward(gradIn.contiguous(), directions, intensites, normals, diffuse))
+class DiffuseShading(_OpFunction):
+    """DiffuseShading.apply(directions, intensities, normals, diffuse)."""
+    op_name = "shade_forward"
 
 
-class LambertShading(th.autograd.Function):
+class LambertShading(_OpFunction):
     """Per-splat Lambert of the forward shading mode (shading.py:12-29),
-    fused into one kernel each way."""
-
-    @staticmethod
-    def forward(ctx, ambient, directions, intensities, normals, diffuse):
-        ts = [t.contiguous() for t in (ambient, directions, intensities, normals, diffuse)]
-        ctx.save_for_backward(*ts)
-        return ops.lambert_forward(*ts)
-
-    @staticmethod
-    def backward(ctx, gradIn):
-        return tuple(ops.lambert_backward(gradIn.contiguous(), *ctx.saved_tensors))
+    one kernel each way: apply(ambient, directions, intensities, normals,
+    diffuse)."""
+    op_name = "lambert_forward"
 
 
-class SphericalHarmonicShading(th.autograd.Function):
-    @staticmethod
-    def forward(ctx, coefficients, normals, diffuse):
-        coefficients, normals, diffuse = coefficients.contiguous(), normals.contiguous(), diffuse.contiguous()
-        ctx.save_for_backward(coefficients, normals, diffuse)
-        return ops.shade_sh_forward(coefficients, normals, diffuse)
-
-    @staticmethod
-    def backward(ctx, gradIn):
-        coefficients, normals, diffuse = ctx.saved_tensors
-        return tuple(ops.shade_sh_backward(gradIn.contiguous(), coefficients, normals, diffuse))
+class SphericalHarmonicShading(_OpFunction):
+    """SphericalHarmonicShading.apply(coefficients, normals, diffuse)."""
+    op_name = "shade_sh_forward"
 
 
 __all__ = ["FmmSampling", "AffineTransform", "LinearTransform", "EWASplatting", "DepthFiltering",
@@ -251,18 +180,8 @@ __all__ = ["FmmSampling", "AffineTransform", "LinearTransform", "EWASplatting", 
 
 
 # ------------------------------------------------------------ pixel gather
-class PixelScatterGather(th.autograd.Function):
+class PixelScatterGather(_OpFunction):
     """extensions/__init__.py:407-437: per-sample splat attributes
     (B,W,H,K,C) from (B,N,C); the backward sums each sample's gradient back
-    onto its splat."""
-
-    @staticmethod
-    def forward(ctx, indices, values):
-        ctx.save_for_backward(indices)
-        ctx.numSources = values.shape[1]
-        return ops.pixel_scatter(indices, values.contiguous())
-
-    @staticmethod
-    def backward(ctx, grad_output):
-        (indices,) = ctx.saved_tensors
-        return None, ops.pixel_gather(indices, grad_output.contiguous(), ctx.numSources, False)
+    onto its splat (apply(indices, values))."""
+    op_name = "pixel_scatter"

@@ -7,9 +7,10 @@ transform.cpp), with a fake (meta) implementation for shape propagation, and
 the differentiable ones with their backward op registered as autograd
 formula, so that ``torch.compile`` traces a render without graph breaks and
 ``torch.library.opcheck`` can check every op.  The gradients registered here
-are the kernels' raw gradients; the reference's post-processing of the EWA
-gradient (norm clamp, NaN scrub, dropped normal gradient) stays in
-``extensions.EWASplatting``.
+are the kernels' raw gradients, except ``ewa_weights``: the EWA weights with
+the reference's post-processing of their gradient (norm clamp, NaN scrub,
+dropped normal gradient), which ``extensions.EWASplatting`` and the renderer
+use.
 
 Schemas use the reference's argument order; names are snake_case
 (``splat_forward`` for ``splatting.forward``).
@@ -84,6 +85,38 @@ def _splat_grad(ctx, grad):
 
 
 splat_forward.register_autograd(_splat_grad, setup_context=_splat_setup)
+
+
+@_op("uds::ewa_weights", mutates_args=())
+def ewa_weights(width: int, height: int, focallength: float, indices: Tensor, points: Tensor, normals: Tensor,
+                stdDevs: Tensor, smoothing: float) -> Tensor:
+    """EWASplatting (extensions/__init__.py:175-233): the weights of
+    splat_forward with the reference's gradient conventions: each splat's
+    point and std-dev gradient scaled to norm <= 1 (conditionalNormalization,
+    utils.py:147-150), NaNs set to 0, no gradient for the normals."""
+    return splatting.forward(width, height, focallength, indices, points, normals, stdDevs, smoothing)
+
+
+@ewa_weights.register_fake
+def _(width, height, focallength, indices, points, normals, stdDevs, smoothing):
+    return points.new_empty(indices.shape)
+
+
+def _clamp_rows(dx: Tensor, eps: float = 1e-4) -> Tensor:
+    return dx / torch.clamp(dx.norm(dim=-1, keepdim=True) + eps, 1.0)
+
+
+def _ewa_grad(ctx, grad):
+    indices, points, normals, stdDevs = ctx.saved_tensors
+    width, height, focallength, smoothing = ctx.args
+    gp, _, gs = torch.ops.uds.splat_backward(width, height, focallength, grad.contiguous(), indices, points, normals,
+                                             stdDevs, smoothing)
+    gp = torch.nan_to_num(_clamp_rows(gp), nan=0.0, posinf=float("inf"), neginf=float("-inf"))
+    gs = torch.nan_to_num(_clamp_rows(gs), nan=0.0, posinf=float("inf"), neginf=float("-inf"))
+    return None, None, None, None, gp, None, gs, None
+
+
+ewa_weights.register_autograd(_ewa_grad, setup_context=_splat_setup)
 
 
 # ------------------------------------------------------------- compositing
@@ -433,7 +466,7 @@ def _(nearest, points, normals, sigma, mean):
     return points.new_empty((2,)), torch.empty_like(points), torch.empty_like(normals)
 
 
-OPS = ("sample", "splat_forward", "splat_backward", "filter_forward", "filter_backward", "interp_forward",
+OPS = ("sample", "splat_forward", "splat_backward", "ewa_weights", "filter_forward", "filter_backward", "interp_forward",
        "interp_backward", "affine_forward", "affine_backward", "linear_forward", "linear_backward",
        "view_matrix_forward", "view_matrix_backward", "backface", "backface_backward", "shade_forward", "shade_backward", "shade_sh_forward",
        "shade_sh_backward", "lambert_forward", "lambert_backward", "pixel_scatter", "pixel_gather", "nearest",
