@@ -292,6 +292,30 @@ int uds_splat_backward(int B, int W, int H, int K, float focal, const float* gra
                        float* grad_points, float* grad_normals, float* grad_std_devs,
                        void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---- The shading pass of Splatting.forward (render.py:268-376, the chain
+ *      splattingCuda.cu:18-66 -> zSortingCuda.cu:11-62 ->
+ *      interpolationCuda.cu:5-46) fused per pixel: EWA weights, depth
+ *      compositing and interpolation of per-splat attributes (aB,N,C), aB in
+ *      {1, B}, in one kernel after the per-splat constants.  Writes the EWA
+ *      weights and depth weights (B,W,H,K) and the image (B,W,H,C),
+ *      bit-identical to uds_splat_forward + uds_filter_forward (points as
+ *      (B,N,3)) + uds_interp_forward.  Workspace: uds_splat_workspace_size.
+ *      The backward takes the gradient of the image and, optionally (NULL:
+ *      none), of the depth weights and of the EWA weights, and the EWA weights
+ *      of the forward; it gives the EWA kernel's raw point / normal / std-dev
+ *      gradients (as uds_splat_backward) and the attribute gradient (aB,N,C),
+ *      the chain's results up to the order of atomic additions. ---- */
+int uds_render_fused_forward(int B, int W, int H, int K, float focal, const int32_t* indices, const float* points,
+                             const float* normals, int std_batch, int N, const float* std_devs, float smoothing,
+                             int aB, int C, const float* attribute, float* weights, float* depth_weights,
+                             float* image, void* workspace, size_t workspace_bytes, void* stream);
+int uds_render_fused_backward(int B, int W, int H, int K, float focal, const float* grad_image,
+                              const float* grad_depth_weights, const float* grad_weights, const int32_t* indices,
+                              const float* weights, const float* points, const float* normals, int std_batch, int N,
+                              const float* std_devs, float smoothing, int aB, int C, const float* attribute,
+                              float* grad_points, float* grad_normals, float* grad_std_devs, float* grad_attribute,
+                              void* workspace, size_t workspace_bytes, void* stream);
+
 /* splatting.forward without a workspace, for callers that cannot allocate
  * device memory (a plugin slot that only passes the op's inputs and outputs,
  * a language binding without a device allocator, a real-time loop that must

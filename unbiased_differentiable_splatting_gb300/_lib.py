@@ -46,6 +46,13 @@ _SIGS = {
     "uds_backface_forward": (c_int, [c_int, c_int, c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "uds_backface_backward": (c_int, [c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p,
                                       c_void_p]),
+    "uds_render_fused_forward": (c_int, [c_int, c_int, c_int, c_int, c_float, c_void_p, c_void_p, c_void_p, c_int,
+                                         c_int, c_void_p, c_float, c_int, c_int, c_void_p, c_void_p, c_void_p,
+                                         c_void_p, c_void_p, c_size_t, c_void_p]),
+    "uds_render_fused_backward": (c_int, [c_int, c_int, c_int, c_int, c_float, c_void_p, c_void_p, c_void_p,
+                                          c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p, c_float,
+                                          c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                          c_size_t, c_void_p]),
     "uds_sample_workspace_size": (c_size_t, [ctypes.POINTER(SampleParams)]),
     "uds_sample": (c_int, [ctypes.POINTER(SampleParams), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                            c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),

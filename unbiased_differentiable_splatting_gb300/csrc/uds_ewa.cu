@@ -9,7 +9,10 @@
 //             rule through covariance, Jacobian, tangent plane and
 //             projection once.  The reference instead runs the full chain
 //             (ewaSplattingGrad.cuh:163-206) per sample and scatters 8 floats.
-#include "uds_ewa.cuh"
+// The fused render kernels at the end of this file run EWA weights, depth
+// compositing and attribute interpolation (and their backward passes) per
+// pixel in one kernel each way.
+#include "uds_composite.cuh"
 
 namespace uds {
 
@@ -208,6 +211,134 @@ __global__ void k_ewa_chain(int B, int N, float W, float H, float f, const float
     }
 }
 
+// ----------------------------------------------------- fused render pass
+// One thread per pixel runs splatting.forward, filtering.forward and
+// interpolation.forward on its K samples (splattingCuda.cu:18-66,
+// zSortingCuda.cu:11-62, interpolationCuda.cu:5-46): EWA weight of each
+// sample from its pair's Gaussian constants, depth along the pixel ray,
+// stable depth order, front-to-back blend, and the blended attributes.  The
+// same device functions in the same order as the three separate kernels, so
+// weights, depth weights and image are bit-identical to them; the (B,W,H,K)
+// intermediates are written once (the autograd needs them) and never read
+// back.
+constexpr int kRenderThreads = 64;
+
+template <int KMAX>
+__global__ void __launch_bounds__(kRenderThreads) k_render_forward(
+    int B, int W, int H, int K, const int* __restrict__ idx, const float4* __restrict__ consts, int N, float f,
+    const float* __restrict__ pts, const float* __restrict__ nrm, int aB, int C, const float* __restrict__ attr,
+    float* __restrict__ w_out, float* __restrict__ dw_out, float* __restrict__ img) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    int i = blockIdx.y, b = blockIdx.z;
+    if (j >= H) return;
+    size_t pix = (size_t)j + (size_t)H * ((size_t)i + (size_t)W * b);
+    size_t e = (size_t)K * pix;
+    float px = (float)i, py = (float)j;
+    const float* bp = pts + 3 * (size_t)N * b;
+    const float* bn = nrm + 3 * (size_t)N * b;
+    float dir[3];
+    pixel_ray((float)W, (float)H, f, px, py, dir);
+    int id[KMAX], ord[KMAX];
+    float wl[KMAX], dist[KMAX], fw[KMAX];
+    for (int k = 0; k < K; ++k) {
+        int s = idx[e + k];
+        bool ok = s >= 0 && s < N;
+        id[k] = ok ? s : -1;
+        float wv = 0.0f;
+        if (ok) {
+            size_t o = (size_t)s + (size_t)N * b;
+            wv = fminf(ewa_gauss(consts[2 * o], consts[2 * o + 1], px, py), 1.0f);
+        }
+        wl[k] = wv;
+        w_out[e + k] = wv;
+        dist[k] = sample_depth(dir, bp, bn, s, N);
+    }
+    depth_order<KMAX>(K, dist, ord);
+    blend<KMAX>(K, ord, wl, fw);
+    for (int k = 0; k < K; ++k) dw_out[e + k] = fw[k];
+    const size_t aoff = aB > 1 ? (size_t)N * b : 0;
+    for (int c0 = 0; c0 < C; c0 += 4) {
+        int cn = min(4, C - c0);
+        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        for (int k = 0; k < K; ++k) {
+            if (id[k] < 0) continue;
+            const float* a = attr + (size_t)C * ((size_t)id[k] + aoff) + c0;
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+                if (c < cn) acc[c] = fadd(acc[c], fmul(fw[k], a[c]));
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+            if (c < cn) img[(size_t)C * pix + c0 + c] = acc[c];
+    }
+}
+
+// The backward of the fused pass per pixel: interpolation.backward (weight
+// gradient per sample, attribute gradient scattered), plus any gradient that
+// reaches the depth weights directly; filtering.backward through the
+// recomputed depth order and blend; and the EWA gradient statistics of
+// k_ewa_stats (gated on the unclamped weight <= 1), plus any gradient that
+// reaches the EWA weights directly.  k_ewa_chain then finishes the splat
+// gradients.  Same arithmetic per sample as the separate kernels; the
+// scattered sums are atomic, as there.
+template <int KMAX>
+__global__ void __launch_bounds__(kRenderThreads) k_render_backward(
+    int B, int W, int H, int K, const float* __restrict__ gimg, const float* __restrict__ gdw_in,
+    const float* __restrict__ gw_in, const int* __restrict__ idx, const float* __restrict__ w,
+    const float4* __restrict__ consts, int N, float f, const float* __restrict__ pts, const float* __restrict__ nrm,
+    int aB, int C, const float* __restrict__ attr, float* __restrict__ ga, float4* __restrict__ stats) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    int i = blockIdx.y, b = blockIdx.z;
+    if (j >= H) return;
+    size_t pix = (size_t)j + (size_t)H * ((size_t)i + (size_t)W * b);
+    size_t e = (size_t)K * pix;
+    float px = (float)i, py = (float)j;
+    const float* bp = pts + 3 * (size_t)N * b;
+    const float* bn = nrm + 3 * (size_t)N * b;
+    float dir[3];
+    pixel_ray((float)W, (float)H, f, px, py, dir);
+    int id[KMAX], ord[KMAX];
+    float wl[KMAX], dist[KMAX], fw[KMAX], gd[KMAX];
+    for (int k = 0; k < K; ++k) {
+        int s = idx[e + k];
+        id[k] = (s >= 0 && s < N) ? s : -1;
+        wl[k] = w[e + k];
+        dist[k] = sample_depth(dir, bp, bn, s, N);
+    }
+    depth_order<KMAX>(K, dist, ord);
+    blend<KMAX>(K, ord, wl, fw);
+    // interpolation.backward with the depth weights fw
+    const float* g = gimg + (size_t)C * pix;
+    const size_t aoff = aB > 1 ? (size_t)N * b : 0;
+    for (int k = 0; k < K; ++k) {
+        float acc = 0.0f;
+        if (id[k] >= 0) {
+            size_t ao = (size_t)C * ((size_t)id[k] + aoff);
+            for (int c = 0; c < C; ++c) {
+                float gi = g[c];
+                atomicAdd(&ga[ao + c], gi * fw[k]);
+                acc = fadd(acc, fmul(gi, attr[ao + c]));
+            }
+        }
+        gd[k] = gdw_in ? fadd(acc, gdw_in[e + k]) : acc;
+    }
+    // filtering.backward, then the EWA statistics in sample order
+    float ge[KMAX];
+    for (int k = 0; k < K; ++k) ge[ord[k]] = blend_grad<KMAX>(K, k, ord, wl, fw, gd);
+    for (int k = 0; k < K; ++k) {
+        if (id[k] < 0) continue;
+        size_t o = (size_t)id[k] + (size_t)N * b;
+        float dx, dy;
+        float G = ewa_gauss(consts[2 * o], consts[2 * o + 1], px, py, &dx, &dy);
+        if (!(G <= 1.0f)) continue;
+        float gk = gw_in ? fadd(ge[k], gw_in[e + k]) : ge[k];
+        float gg = gk * G;
+        if (gg == 0.0f) continue;
+        atomicAdd(&stats[2 * o], make_float4(gg, gg * dx, gg * dy, gg * dx * dx));
+        atomicAdd(reinterpret_cast<float2*>(&stats[2 * o + 1]), make_float2(gg * dx * dy, gg * dy * dy));
+    }
+}
+
 }  // namespace uds
 
 using namespace uds;
@@ -280,5 +411,85 @@ extern "C" int uds_splat_backward(int B, int W, int H, int K, float focal, const
     k_ewa_chain<<<dim3(cdiv(N, 128), B), 128, 0, s>>>(B, N, (float)W, (float)H, focal, points, normals,
                                                      std_devs, std_batch, smoothing, stats, grad_points,
                                                      grad_normals, grad_std_devs);
+    return launch_status();
+}
+
+#define UDS_RENDER_DISPATCH(KERNEL, ...)                                               \
+    do {                                                                                 \
+        dim3 grid(cdiv(H, kRenderThreads), W, B);                                        \
+        if (K <= 8) KERNEL<8><<<grid, kRenderThreads, 0, s>>>(__VA_ARGS__);              \
+        else if (K <= 16) KERNEL<16><<<grid, kRenderThreads, 0, s>>>(__VA_ARGS__);       \
+        else if (K <= 32) KERNEL<32><<<grid, kRenderThreads, 0, s>>>(__VA_ARGS__);       \
+        else KERNEL<64><<<grid, kRenderThreads, 0, s>>>(__VA_ARGS__);                    \
+    } while (0)
+
+// Sampled-pair flags and Gaussian constants in the splat workspace (the
+// first step of uds_splat_forward / backward).
+static int render_consts(int B, int W, int H, int K, float focal, const int32_t* indices, const float* points,
+                         const float* normals, int std_batch, int N, const float* std_devs, float smoothing,
+                         void* workspace, cudaStream_t s) {
+    float4* consts = reinterpret_cast<float4*>(workspace);
+    unsigned char* used = reinterpret_cast<unsigned char*>(workspace) + 2 * align256(sizeof(float4) * 2 * (size_t)B * N);
+    cudaError_t e = cudaMemsetAsync(used, 0, (size_t)B * N, s);
+    if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
+    k_ewa_mark<<<dim3(cdiv(H, 64), W, B), 64, 0, s>>>(B, W, H, K, indices, N, used);
+    k_ewa_consts<<<dim3(cdiv(N, 128), B), 128, 0, s>>>(B, N, (float)W, (float)H, focal, points, normals, std_devs,
+                                                      std_batch, smoothing, used, consts);
+    return launch_status(2);
+}
+
+extern "C" int uds_render_fused_forward(int B, int W, int H, int K, float focal, const int32_t* indices,
+                                        const float* points, const float* normals, int std_batch, int N,
+                                        const float* std_devs, float smoothing, int aB, int C,
+                                        const float* attribute, float* weights, float* depth_weights, float* image,
+                                        void* workspace, size_t workspace_bytes, void* stream) {
+    int st = check_splat_args(B, W, H, K, std_batch, N);
+    if (st) return st;
+    if (K > kMaxK || C <= 0 || (aB != 1 && aB != B) || !indices || !weights || !depth_weights || !image ||
+        (N > 0 && (!points || !normals || !std_devs || !attribute)))
+        return UDS_ERR_ARGUMENT;
+    if (workspace_bytes < uds_splat_workspace_size(B, N) || (N > 0 && !workspace)) return UDS_ERR_WORKSPACE;
+    cudaStream_t s = as_stream(stream);
+    if (N > 0 && (st = render_consts(B, W, H, K, focal, indices, points, normals, std_batch, N, std_devs, smoothing,
+                                     workspace, s)))
+        return st;
+    const float4* consts = reinterpret_cast<const float4*>(workspace);
+    UDS_RENDER_DISPATCH(k_render_forward, B, W, H, K, indices, consts, N, focal, points, normals, aB, C, attribute,
+                        weights, depth_weights, image);
+    return launch_status();
+}
+
+extern "C" int uds_render_fused_backward(int B, int W, int H, int K, float focal, const float* grad_image,
+                                         const float* grad_depth_weights, const float* grad_weights,
+                                         const int32_t* indices, const float* weights, const float* points,
+                                         const float* normals, int std_batch, int N, const float* std_devs,
+                                         float smoothing, int aB, int C, const float* attribute, float* grad_points,
+                                         float* grad_normals, float* grad_std_devs, float* grad_attribute,
+                                         void* workspace, size_t workspace_bytes, void* stream) {
+    int st = check_splat_args(B, W, H, K, std_batch, N);
+    if (st) return st;
+    if (K > kMaxK || C <= 0 || (aB != 1 && aB != B) || !grad_image || !indices || !weights) return UDS_ERR_ARGUMENT;
+    if (N > 0 && (!points || !normals || !std_devs || !attribute || !grad_points || !grad_normals || !grad_std_devs ||
+                  !grad_attribute))
+        return UDS_ERR_ARGUMENT;
+    if (workspace_bytes < uds_splat_workspace_size(B, N) || (N > 0 && !workspace)) return UDS_ERR_WORKSPACE;
+    if (N == 0) return UDS_OK;
+    cudaStream_t s = as_stream(stream);
+    float4* stats = reinterpret_cast<float4*>(reinterpret_cast<char*>(workspace) +
+                                              align256(sizeof(float4) * 2 * (size_t)B * N));
+    cudaError_t e = cudaMemsetAsync(stats, 0, sizeof(float4) * 2 * (size_t)B * N, s);
+    if (e == cudaSuccess && std_batch == 1) e = cudaMemsetAsync(grad_std_devs, 0, sizeof(float) * 2 * (size_t)N, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(grad_attribute, 0, sizeof(float) * (size_t)aB * N * C, s);
+    if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
+    if ((st = render_consts(B, W, H, K, focal, indices, points, normals, std_batch, N, std_devs, smoothing, workspace,
+                            s)))
+        return st;
+    const float4* consts = reinterpret_cast<const float4*>(workspace);
+    UDS_RENDER_DISPATCH(k_render_backward, B, W, H, K, grad_image, grad_depth_weights, grad_weights, indices, weights,
+                        consts, N, focal, points, normals, aB, C, attribute, grad_attribute, stats);
+    if ((st = launch_status())) return st;
+    k_ewa_chain<<<dim3(cdiv(N, 128), B), 128, 0, s>>>(B, N, (float)W, (float)H, focal, points, normals, std_devs,
+                                                     std_batch, smoothing, stats, grad_points, grad_normals,
+                                                     grad_std_devs);
     return launch_status();
 }

@@ -5,41 +5,11 @@
 // blending and its division-based gradient.  The arithmetic follows the
 // reference operation by operation (double where it promotes), so the depth
 // order is identical to the CPU oracle's.
-#include "uds_ewa.cuh"
+#include "uds_composite.cuh"
 
 namespace uds {
 
 constexpr int kFilterThreads = 64;
-
-// -normalize(backproject(pixel)) (alphacompositing.cuh:31-32)
-__device__ __forceinline__ void pixel_ray(float W, float H, float f, float px, float py, float* dir) {
-    float s[2] = {px, py}, wd[3];
-    back_project(W, H, f, s, wd);
-    float inv = div_via_double(1.0f, fsqrt(dot3(wd, wd)));
-#pragma unroll
-    for (int i = 0; i < 3; ++i) dir[i] = fmul(fmul(wd[i], inv), -1.0f);
-}
-
-__device__ __forceinline__ float sample_depth(const float* dir, const float* __restrict__ pts,
-                                              const float* __restrict__ nrm, int id, int N) {
-    if (id < 0 || id >= N) return kZmax;
-    float p[3] = {pts[3 * (size_t)id], pts[3 * (size_t)id + 1], pts[3 * (size_t)id + 2]};
-    float n[3] = {nrm[3 * (size_t)id], nrm[3 * (size_t)id + 1], nrm[3 * (size_t)id + 2]};
-    float d = fdiv(dot3(p, n), dot3(dir, n));
-    return d > 0.0f ? d : kZmax;
-}
-
-template <int KMAX>
-__device__ __forceinline__ void depth_order(int K, const float* dist, int* ord) {
-    for (int i = 0; i < K; ++i) ord[i] = i;
-    for (int i = 1; i < K; ++i) {
-        int index = ord[i];
-        float value = dist[index];
-        int j = i;
-        while (j > 0 && dist[ord[j - 1]] > value) { ord[j] = ord[j - 1]; --j; }
-        ord[j] = index;
-    }
-}
 
 template <int KMAX>
 __global__ void k_filter_forward(int B, int W, int H, int K, const int* __restrict__ idx,
@@ -57,13 +27,10 @@ __global__ void k_filter_forward(int B, int W, int H, int K, const int* __restri
     int ord[KMAX];
     for (int k = 0; k < K; ++k) dist[k] = sample_depth(dir, pts + po, nrm + po, idx[e + k], N);
     depth_order<KMAX>(K, dist, ord);
-    float rem = 1.0f;
-    for (int q = 0; q < K; ++q) {
-        int id = ord[q];
-        float wt = w[e + id];
-        out[e + id] = fmul(rem, wt);
-        rem = (float)dmul((double)rem, dsub(1.0, (double)wt));
-    }
+    float wl[KMAX], fw[KMAX];
+    for (int k = 0; k < K; ++k) wl[k] = w[e + k];
+    blend<KMAX>(K, ord, wl, fw);
+    for (int k = 0; k < K; ++k) out[e + k] = fw[k];
 }
 
 template <int KMAX>
@@ -78,31 +45,16 @@ __global__ void k_filter_backward(int B, int W, int H, int K, const int* __restr
     size_t po = pB > 1 ? 3 * (size_t)N * b : 0;
     float dir[3];
     pixel_ray((float)W, (float)H, f, (float)i, (float)j, dir);
-    float dist[KMAX], fw[KMAX], wl[KMAX];
+    float dist[KMAX], fw[KMAX], wl[KMAX], gl[KMAX];
     int ord[KMAX];
     for (int k = 0; k < K; ++k) {
         dist[k] = sample_depth(dir, pts + po, nrm + po, idx[e + k], N);
         wl[k] = w[e + k];
+        gl[k] = gin[e + k];
     }
     depth_order<KMAX>(K, dist, ord);
-    float rem = 1.0f;
-    for (int q = 0; q < K; ++q) {
-        int id = ord[q];
-        fw[id] = fmul(rem, wl[id]);
-        rem = (float)dmul((double)rem, dsub(1.0, (double)wl[id]));
-    }
-    const float eps = 1e-4f;
-    for (int k = 0; k < K; ++k) {
-        int kdx = ord[k];
-        float wk = wl[kdx];
-        float g = 0.0f;
-        for (int q = k; q < K; ++q) {
-            int id = ord[q];
-            float den = (q == k) ? wk : -fsub(1.0f, wk);
-            if (fabsf(den) > eps) g = fadd(g, fdiv(fmul(gin[e + id], fw[id]), den));
-        }
-        out[e + kdx] = g;
-    }
+    blend<KMAX>(K, ord, wl, fw);
+    for (int k = 0; k < K; ++k) out[e + ord[k]] = blend_grad<KMAX>(K, k, ord, wl, fw, gl);
 }
 
 }  // namespace uds

@@ -119,6 +119,66 @@ def _ewa_grad(ctx, grad):
 ewa_weights.register_autograd(_ewa_grad, setup_context=_splat_setup)
 
 
+@_op("uds::render_splats", mutates_args=())
+def render_splats(width: int, height: int, focallength: float, indices: Tensor, points: Tensor, normals: Tensor,
+                  stdDevs: Tensor, smoothing: float, attribute: Tensor) -> Tuple[Tensor, Tensor, Tensor]:
+    """EWA weights -> depth compositing -> interpolation of the per-splat
+    attribute (1|B,N,C) in one fused pass: (image (B,W,H,C), depth weights,
+    EWA weights), bit-identical to ewa_weights, filter_forward and
+    interp_forward.  Gradients as that chain: the EWA part with the
+    reference's post-processing (ewa_weights), none for the normals."""
+    image, depth, weights = splatting.renderForward(width, height, focallength, indices, points, normals, stdDevs,
+                                                    smoothing, attribute)
+    return image, depth, weights
+
+
+@render_splats.register_fake
+def _(width, height, focallength, indices, points, normals, stdDevs, smoothing, attribute):
+    B, W, H, _ = indices.shape
+    return (points.new_empty((B, W, H, attribute.shape[2])), points.new_empty(indices.shape),
+            points.new_empty(indices.shape))
+
+
+@_op("uds::render_splats_backward", mutates_args=())
+def render_splats_backward(width: int, height: int, focallength: float, gradImage: Tensor,
+                           gradDepthWeights: Optional[Tensor], gradWeights: Optional[Tensor], indices: Tensor,
+                           weights: Tensor, points: Tensor, normals: Tensor, stdDevs: Tensor, smoothing: float,
+                           attribute: Tensor) -> List[Tensor]:
+    """Raw gradients of render_splats: [points, normals, std-devs, attribute]."""
+    return splatting.renderBackward(width, height, focallength, gradImage, gradDepthWeights, gradWeights, indices,
+                                    weights, points, normals, stdDevs, smoothing, attribute)
+
+
+@render_splats_backward.register_fake
+def _(width, height, focallength, gradImage, gradDepthWeights, gradWeights, indices, weights, points, normals,
+      stdDevs, smoothing, attribute):
+    return [torch.empty_like(t) for t in (points, normals, stdDevs, attribute)]
+
+
+def _render_setup(ctx, inputs, output):
+    width, height, focallength, indices, points, normals, stdDevs, smoothing, attribute = inputs
+    ctx.save_for_backward(indices, points, normals, stdDevs, attribute, output[2])
+    ctx.args = (width, height, focallength, smoothing)
+    ctx.image_shape = output[0].shape
+
+
+def _render_grad(ctx, g_image, g_depth, g_weights):
+    indices, points, normals, stdDevs, attribute, weights = ctx.saved_tensors
+    width, height, focallength, smoothing = ctx.args
+    if g_image is None:
+        g_image = weights.new_zeros(ctx.image_shape)
+    c = lambda t: None if t is None else t.contiguous()  # noqa: E731
+    gp, _, gs, ga = torch.ops.uds.render_splats_backward(width, height, focallength, g_image.contiguous(),
+                                                         c(g_depth), c(g_weights), indices, weights, points,
+                                                         normals, stdDevs, smoothing, attribute)
+    gp = torch.nan_to_num(_clamp_rows(gp), nan=0.0, posinf=float("inf"), neginf=float("-inf"))
+    gs = torch.nan_to_num(_clamp_rows(gs), nan=0.0, posinf=float("inf"), neginf=float("-inf"))
+    return None, None, None, None, gp, None, gs, None, ga
+
+
+render_splats.register_autograd(_render_grad, setup_context=_render_setup)
+
+
 # ------------------------------------------------------------- compositing
 @_op("uds::filter_forward", mutates_args=())
 def filter_forward(indices: Tensor, weights: Tensor, width: int, height: int, focallength: float, points: Tensor,
@@ -466,7 +526,7 @@ def _(nearest, points, normals, sigma, mean):
     return points.new_empty((2,)), torch.empty_like(points), torch.empty_like(normals)
 
 
-OPS = ("sample", "splat_forward", "splat_backward", "ewa_weights", "filter_forward", "filter_backward", "interp_forward",
+OPS = ("sample", "splat_forward", "splat_backward", "ewa_weights", "render_splats", "render_splats_backward", "filter_forward", "filter_backward", "interp_forward",
        "interp_backward", "affine_forward", "affine_backward", "linear_forward", "linear_backward",
        "view_matrix_forward", "view_matrix_backward", "backface", "backface_backward", "shade_forward", "shade_backward", "shade_sh_forward",
        "shade_sh_backward", "lambert_forward", "lambert_backward", "pixel_scatter", "pixel_gather", "nearest",

@@ -5,7 +5,10 @@
 ``Splatting.forward`` runs: world->camera transform of points and normals,
 back-face orientation, FMM sampling of K splats per pixel, EWA weights, depth
 compositing, shading / attribute interpolation.  Every stage is a CUDA op of
-libuds.so behind the autograd wrappers of ``extensions``.
+libuds.so behind the autograd wrappers of ``extensions``; for the shading
+modes that interpolate one per-splat attribute (forward, forwardHarmonics,
+None) the EWA weights, compositing and interpolation run as one fused kernel
+each way (``torch.ops.uds.render_splats``), with the same results.
 
 Difference from the reference: ``self.indices`` (render.py:296 copies the
 indices to the host on every forward) is a lazy property here, so a forward
@@ -112,6 +115,12 @@ class DeferredSphericalHaromic(th.nn.Module):
         return SphericalHarmonicShading.apply(self.coefficients, normals, diffuse)
 
 
+def _fusable(attribute: th.Tensor, camPoints: th.Tensor) -> bool:
+    return (isinstance(attribute, th.Tensor) and attribute.is_cuda and attribute.dtype == th.float32
+            and attribute.device == camPoints.device and attribute.dim() == 3
+            and attribute.shape[1] == camPoints.shape[1] and attribute.shape[0] in (1, camPoints.shape[0]))
+
+
 def _normalizeNormals(normals: th.Tensor) -> th.Tensor:
     norms = normals.norm(dim=-1, keepdim=True)
     normals = th.where(norms < 0.01, th.ones_like(normals), normals)
@@ -146,6 +155,9 @@ class Splatting(th.nn.Module):
         self.sphericalHarmonics = DeferredSphericalHaromic()
         self.forwardHarmonics = ForwardSphericalHaromic()
         self.sample_kwargs = {}
+        # per-splat shading modes run the fused render kernels (False: the
+        # separate EWA / compositing / interpolation ops, same results)
+        self.fused = True
         self._indices = None
 
     @property
@@ -167,28 +179,35 @@ class Splatting(th.nn.Module):
                                     backfaceNormals.detach().contiguous(), pointDiffuse, pointStdDevs.detach(),
                                     self.numSamples, self.smoothing, self.precision, **self.sample_kwargs)
         self._indices = indices
+        camLampDirections = self.linearTransform(transformMatrix, lampDirections)
+        # the modes that interpolate one per-splat attribute
+        perSplat = None
+        if self.shadingMode == "forward":
+            perSplat = self.forwardShading(ambientLight, camLampDirections, lampIntensities, camNormals, pointDiffuse)
+        elif self.shadingMode == "forwardHarmonics":
+            perSplat = self.forwardHarmonics(pointNormals, pointDiffuse)
+        elif self.shadingMode == "None":
+            perSplat = pointDiffuse
+        if perSplat is not None and self.fused and _fusable(perSplat, camPoints):
+            # EWA -> compositing -> interpolation in one kernel each way
+            image, depthWeights, _ = th.ops.uds.render_splats(
+                self.width, self.height, self.focallength, indices, camPoints.contiguous(), camNormals.contiguous(),
+                pointStdDevs.contiguous(), self.smoothing, perSplat.contiguous())
+            return image, indices, depthWeights
         ewaWeights = self.ewa(self.width, self.height, self.focallength, indices, camPoints, camNormals, pointStdDevs,
                               self.smoothing)
         depthWeights = self.depthBlending(indices, ewaWeights, self.width, self.height, self.focallength, camPoints,
                                           camNormals)
-        camLampDirections = self.linearTransform(transformMatrix, lampDirections)
         if self.shadingMode == "deferred":
             ewaNormals = _normalizeNormals(self.linearInterpolation(indices, depthWeights, camNormals))
             ewaDiffuse = self.linearInterpolation(indices, depthWeights, pointDiffuse)
             image = self.deferredShading(camLampDirections, lampIntensities, ewaNormals.contiguous(), ewaDiffuse)
-        elif self.shadingMode == "forward":
-            shadedPoints = self.forwardShading(ambientLight, camLampDirections, lampIntensities, camNormals,
-                                               pointDiffuse)
-            image = self.linearInterpolation(indices, depthWeights, shadedPoints)
+        elif perSplat is not None:
+            image = self.linearInterpolation(indices, depthWeights, perSplat)
         elif self.shadingMode == "sphericalHarmonics":
             ewaNormals = self.linearInterpolation(indices, depthWeights, pointNormals)
             ewaDiffuse = self.linearInterpolation(indices, depthWeights, pointDiffuse)
             image = self.sphericalHarmonics(ewaNormals, ewaDiffuse)
-        elif self.shadingMode == "forwardHarmonics":
-            shadedPoints = self.forwardHarmonics(pointNormals, pointDiffuse)
-            image = self.linearInterpolation(indices, depthWeights, shadedPoints)
-        elif self.shadingMode == "None":
-            image = self.linearInterpolation(indices, depthWeights, pointDiffuse)
         elif self.shadingMode == "silhouette":
             image = th.clamp(th.sum(ewaWeights, dim=-1, keepdim=True), 0, 1)
         else:
