@@ -1167,23 +1167,17 @@ __global__ void __launch_bounds__(128, 4) k_sample(Tree T, const ViewState* vs, 
                     need = true;
                 }
             }
-            // lanes at the same node evaluate its children's masses together
-            unsigned pend = __ballot_sync(full, need);
-            while (pend) {
-                int leader = __ffs(pend) - 1;
-                int vv = __shfl_sync(full, v, leader);
-                bool mineg = need && v == vv;
-                unsigned grp = __ballot_sync(full, mineg);
-                if (mineg) {
-                    // one call site: the walk is inlined once, which keeps the
-                    // kernel's hot code small enough for the instruction cache
+            // every lane that needs its node's child masses evaluates them
+            // at once, whatever node it is at (below the expansion frontier a
+            // child is one expansion, so the divergence is only in the
+            // series' trip counts); one call site keeps the walk inlined once,
+            // small enough for the instruction cache
+            if (need) {
 #pragma unroll 1
-                    for (int ch = 0; ch < 2; ++ch) {
-                        float x = fmaxf(0.0f, node_weight(T, ch ? b : a, qx, qy));
-                        if (ch) w1 = x; else w0 = x;
-                    }
+                for (int ch = 0; ch < 2; ++ch) {
+                    float x = fmaxf(0.0f, node_weight(T, ch ? b : a, qx, qy));
+                    if (ch) w1 = x; else w0 = x;
                 }
-                pend &= ~grp;
             }
             if (going) {
                 // (re)write unconditionally: a hit stores the same masses, and
@@ -1300,7 +1294,7 @@ __global__ void __launch_bounds__(128, 4) k_stochastic(Tree T, const ViewState* 
     // same warp layout and per-pixel mass cache as k_sample: one warp walks
     // its 32 pixels' trees together, then every lane draws its K paths; the
     // masses come from the cache, the per-depth cache of earlier draws, or a
-    // grouped evaluation by the lanes at the same node (all bit-identical to
+    // direct evaluation by each lane that needs them (all bit-identical to
     // separate getWeight calls)
     if (seed_ptr) seed = *seed_ptr;
     __shared__ WalkStack s_walk[4];
@@ -1356,22 +1350,14 @@ __global__ void __launch_bounds__(128, 4) k_stochastic(Tree T, const ViewState* 
                     need = true;
                 }
             }
-            unsigned pend = __ballot_sync(full, need);
-            while (pend) {
-                int leader = __ffs(pend) - 1;
-                int vv = __shfl_sync(full, v, leader);
-                bool mineg = need && v == vv;
-                unsigned grp = __ballot_sync(full, mineg);
-                if (mineg) {
-                    // one call site: the walk is inlined once, which keeps the
-                    // kernel's hot code small enough for the instruction cache
+            // every lane that needs its node's child masses evaluates them
+            // at once (one call site: the walk is inlined once)
+            if (need) {
 #pragma unroll 1
-                    for (int ch = 0; ch < 2; ++ch) {
-                        float x = fmaxf(0.0f, node_weight(T, ch ? b : a, qx, qy));
-                        if (ch) w1 = x; else w0 = x;
-                    }
+                for (int ch = 0; ch < 2; ++ch) {
+                    float x = fmaxf(0.0f, node_weight(T, ch ? b : a, qx, qy));
+                    if (ch) w1 = x; else w0 = x;
                 }
-                pend &= ~grp;
             }
             if (going) {
                 cv[d] = v;
