@@ -203,13 +203,15 @@ def cpu_baseline(wl, scene):
             "fp32_fgt": {"value": S / t32 / 1e6, "seconds": t32, "sample": CPU_SAMPLE["fp32"].format(W=W, H=W)}}
 
 
-def profiled_traffic(kernel="k_sample"):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary of the
-    current build (the line `traffic_bytes_per_launch <kernel>: <bytes>`)."""
+def profiled(key, kernel="k_sample"):
+    """A per-launch figure of `kernel` from the committed ncu summary of the
+    current build (the line `<key> <kernel>: <value>`): DRAM bytes
+    (traffic_bytes_per_launch) or warp instructions
+    (warp_instructions_per_launch)."""
     path = os.path.join(ROOT, "profiles", "k_sample_harmonic500k_1024.md")
     try:
         for line in open(path):
-            if line.startswith(f"traffic_bytes_per_launch {kernel}:"):
+            if line.startswith(f"{key} {kernel}:"):
                 return int(line.split(":")[1])
     except OSError:
         pass
@@ -381,17 +383,23 @@ def multiview_main(args, name, wl):
         else None, "clocks": clk, "gpu_launches": int(launches)}), flush=True)
 
 
-def proposal_main(args):
+def proposal_record(train_steps=1000, seeds=16, rows=10_000_000):
     """Learned proposal against the plain stochastic sampler on the 500k /
-    1024^2 / K=8 view: time per sampling call (CUDA events, device-resident
-    inputs), per-pixel variance of the weighted image estimate over seeds, and
-    the wall time the learned sampler needs to reach the plain sampler's
-    variance (variance scales as 1 / draws)."""
+    1024^2 / K=8 view, on the quantity training uses: the per-splat gradient
+    of a loss through the weighted image estimate.  With a fixed upstream
+    gradient g (seeded N(0,1) per pixel and channel, standing in for
+    dL/dimage), splat j's albedo gradient is sum_{pixel,k: j_k = j} g w_k / K;
+    its variance over seeds (trace over the 3 channels, mean over the splats
+    that receive one) and the time per sampling call give the time each
+    method needs for a given variance (variance ~ 1 / draws).  The mean over
+    seeds on a 64 x 64 crop is compared with the exact expectation
+    sum_pixel g p_j(pixel), p_j = G_j / sum_i G_i, summed directly in FP64
+    (bias, with the Monte-Carlo error beside it).  The network trains on
+    `rows` descent decisions of the sampler itself."""
     import torch
-    from unbiased_differentiable_splatting_gb300 import load, proposal, scenes
+    from unbiased_differentiable_splatting_gb300 import proposal
+    from unbiased_differentiable_splatting_gb300.cudaExtensions import pixelgather, sampling, transform
     from unbiased_differentiable_splatting_gb300.extensions import transformForward, world2Camera
-    from unbiased_differentiable_splatting_gb300.cudaExtensions import transform
-    L = load()
     dev = torch.device("cuda", 0)
     wl = WORKLOADS["harmonic500k"]
     sc = make_scene(wl)
@@ -404,34 +412,99 @@ def proposal_main(args):
         cn = transform.linearForward(M, d["normals"])
         cnb = torch.where(cn[..., 2:] > 0, -cn, cn).contiguous()
     args_ = (W, H, sc["focal"], cp, cnb, d["stddevs"])
-    values = d["colors"][..., :1].contiguous()
+    N = cp.shape[1]
     stream = torch.cuda.current_stream(dev)
+    gen = torch.Generator(device=dev).manual_seed(7)
+    g_full = torch.randn((1, W, H, 3), device=dev, generator=gen)
+    c0 = W // 2 - 32
+    crop = torch.zeros((1, W, H, 1), device=dev)
+    crop[:, c0:c0 + 64, c0:c0 + 64] = 1.0
+    g_crop = g_full * crop
 
-    def timed(net, seeds):
-        out, ts = [], []
-        for s in seeds:
+    # training on the sampler's own decisions
+    t0 = time.perf_counter()
+    X, tgt = proposal.dataset(*args_, 0.0, prec, stride=2, draws=8, cap=rows, seed=11)
+    net = proposal.ProposalNet(dev, seed=0)
+    losses = net.train(X, tgt, steps=train_steps, batch=65536, lr=3e-3)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+
+    def grads(idx, w, g):
+        vals = (g[:, :, :, None, :] * torch.where(idx >= 0, w, torch.zeros_like(w))[..., None] / K).contiguous()
+        return pixelgather.gather(idx, vals, N, True)[0]  # (N, 3)
+
+    def run(net_, ss):
+        full, part, ts, nfb = [], [], [], 0
+        for s_ in ss:
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            idx, w, fb, nfb = proposal.sample(*args_, K, 0.0, prec, net=net, ess_tau=0.1, seed=s)
+            idx, w, fb, n_fb = proposal.sample(*args_, K, 0.0, prec, net=net_, ess_tau=0.1, seed=s_)
             e1.record(stream)
             e1.synchronize()
             ts.append(e0.elapsed_time(e1))
-            out.append((proposal.estimate(idx, w, values)[0, ..., 0], int(nfb.sum())))
-        return out, ts
+            full.append(grads(idx, w, g_full))
+            part.append(grads(idx, w, g_crop))
+            nfb += int(n_fb.sum())
+        return torch.stack(full), torch.stack(part), float(np.median(ts)), nfb / len(ss)
 
-    # training: rows from the sampler itself, then Adam on the tensor cores
-    t0 = time.perf_counter()
-    X, tgt = proposal.dataset(*args_, 0.0, prec, stride=4, draws=8, seed=11)
+    seed_list = list(range(100, 100 + seeds))
+    run(None, seed_list[:2])
+    run(net, seed_list[:2])
+    fp, cp_, tp, _ = run(None, seed_list)
+    fl, cl, tl_, nfb_l = run(net, seed_list)
+
+    # exact expectation on the crop, FP64 direct Gauss sums over the leaves
+    tree = sampling.build_tree(W, H, sc["focal"], cp, cnb, d["stddevs"], K, 0.0, prec)
+    n = tree["n_visible"]
+    h = tree["h"]
+    xy = tree["centre"][n - 1:].to(dev).double()
+    ids = tree["ids"].to(dev).long()
+    near = ((xy[:, 0] > c0 - 8) & (xy[:, 0] < c0 + 72) & (xy[:, 1] > c0 - 8) & (xy[:, 1] < c0 + 72))
+    xy, ids = xy[near], ids[near]
+    gi, gj = torch.meshgrid(torch.arange(c0, c0 + 64, device=dev, dtype=torch.float64),
+                            torch.arange(c0, c0 + 64, device=dev, dtype=torch.float64), indexing="ij")
+    d2 = (gi.reshape(-1, 1) - xy[:, 0]) ** 2 + (gj.reshape(-1, 1) - xy[:, 1]) ** 2
+    G = torch.exp(-d2 / (2.0 * h * h))
+    Pm = G / G.sum(1, keepdim=True)
+    gc = g_full[0, c0:c0 + 64, c0:c0 + 64].reshape(-1, 3).double()
+    exact = torch.zeros((N, 3), device=dev, dtype=torch.float64)
+    exact.index_add_(0, ids, Pm.t() @ gc)
+
+    def stats(fullg, cropg, t_ms):
+        live = fullg.abs().sum((0, 2)) > 0
+        var = float(fullg.double().var(0).sum(1)[live].mean())
+        mean = cropg.double().mean(0)
+        en = float(exact.norm())
+        bias = float((mean - exact).norm()) / en
+        mc = float((cropg.double().var(0).sum() / cropg.shape[0]).sqrt()) / en
+        return {"ms_per_call": t_ms, "grad_variance": var, "crop_bias_rel": bias, "crop_mc_error_rel": mc}
+
+    sp, sl = stats(fp, cp_, tp), stats(fl, cl, tl_)
+    sl["fallback_pixels_per_call"] = nfb_l
+    ratio = (sl["ms_per_call"] * sl["grad_variance"]) / (sp["ms_per_call"] * sp["grad_variance"])
+    return {"metric": "time to the plain sampler's gradient variance, learned / plain", "value": ratio,
+            "unit": "ratio", "higher_is_better": False, "target": 0.5, "seeds": seeds,
+            "upstream": "seeded N(0,1) per pixel and channel; albedo gradients per splat",
+            "plain": sp, "learned": sl,
+            "train": {"rows": int(X.shape[0]), "steps": train_steps, "batch": 65536, "seconds": t_train,
+                      "final_loss": float(losses[-20:].mean())}}
+
+
+def proposal_main(args):
+    """The learned-proposal record alone (it is also part of the default
+    line), plus the tensor-core throughput of the network on 4M rows."""
+    import torch
+    from unbiased_differentiable_splatting_gb300 import load, proposal
+    load()
+    dev = torch.device("cuda", 0)
+    rec = proposal_record(train_steps=args.train_steps, seeds=args.seeds)
     net = proposal.ProposalNet(dev, seed=0)
-    losses = net.train(X, tgt, steps=args.train_steps, batch=65536, lr=3e-3)
-    torch.cuda.synchronize()
-    t_train = time.perf_counter() - t0
-    # tensor-core throughput of the network alone on 4M rows
     R = 1 << 22
     Xr = torch.randn(R, 16, device=dev)
     for _ in range(2):
         net.logits(Xr)
+    stream = torch.cuda.current_stream(dev)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
@@ -440,34 +513,12 @@ def proposal_main(args):
     e1.synchronize()
     t_mlp = e0.elapsed_time(e1) * 1e-3
     flops = 2.0 * R * (16 * 64 + 64 * 64 * 2 + 64 * 16)
-    seeds = list(range(100, 100 + args.seeds))
-    timed(None, seeds[:2])
-    timed(net, seeds[:2])
-    plain, tp = timed(None, seeds)
-    learned, tl = timed(net, seeds)
-    ep = torch.stack([e for e, _ in plain])
-    el = torch.stack([e for e, _ in learned])
-    live = ep.mean(0) != 0
-    var_p = float(ep.var(0)[live].mean())
-    var_l = float(el.var(0)[live].mean())
-    t_p, t_l = float(np.median(tp)), float(np.median(tl))
     peaks = os.path.join(ROOT, "MEASURED_PEAKS.json")
     bf16_peak = json.load(open(peaks)).get("bf16_tflops") if os.path.exists(peaks) else None
-    print(json.dumps({
-        "metric": "time to the plain sampler's estimator variance, learned / plain", "value": (t_l * var_l / var_p) / t_p,
-        "unit": "ratio", "higher_is_better": False, "n_gpus": 1, "dtype": "bf16 network, f32 sampler",
-        "data": "synthetic", "config": {"workload": workload_name("harmonic500k", wl), "seeds": args.seeds,
-                                        "estimate": "weighted mean of the splat albedo (channel 0) per pixel",
-                                        "ess_tau": 0.1},
-        "plain": {"ms_per_call": t_p, "variance": var_p},
-        "learned": {"ms_per_call": t_l, "variance": var_l,
-                    "fallback_pixels_per_call": float(np.mean([n for _, n in learned])),
-                    "train_rows": int(X.shape[0]), "train_steps": args.train_steps, "train_s": t_train,
-                    "final_loss": float(losses[-10:].mean())},
-        "network_tensor_cores": {"rows": R, "ms": t_mlp * 1e3, "tflops": flops / t_mlp / 1e12,
-                                 "peak_bf16_tflops": bf16_peak,
-                                 "frac": (flops / t_mlp / 1e12) / bf16_peak if bf16_peak else None},
-    }), flush=True)
+    rec["network_tensor_cores"] = {"rows": R, "ms": t_mlp * 1e3, "tflops": flops / t_mlp / 1e12,
+                                   "peak_bf16_tflops": bf16_peak,
+                                   "frac": (flops / t_mlp / 1e12) / bf16_peak if bf16_peak else None}
+    print(json.dumps(rec), flush=True)
 
 
 def next_rows_main(args):
@@ -558,6 +609,60 @@ def next_rows_main(args):
                       "l2": "flushed (256 MiB write) before each call", "rows": rows}), flush=True)
 
 
+def descent_main(args):
+    """The per-pixel descent kernel alone on the harmonic 500k / 1024^2 view
+    (the tree built once, then --warmup untimed and --steps timed launches
+    with the tile the autotuner caches, else 8 pixels wide): the small,
+    self-contained command the ncu captures of k_sample run on."""
+    import torch
+    from unbiased_differentiable_splatting_gb300 import _lib, autotune, load
+    from unbiased_differentiable_splatting_gb300.extensions import transformForward, world2Camera
+    from unbiased_differentiable_splatting_gb300.cudaExtensions import sampling, transform
+    if args.impl == "reference":
+        print(json.dumps({"impl": "reference", "unavailable": "the descent-only mode times this build's kernel"}))
+        return
+    L = load()
+    dev = torch.device("cuda", 0)
+    wl = WORKLOADS["harmonic500k"]
+    sc = make_scene(wl)
+    W = H = wl["width"]
+    K = wl["K"]
+    d = {k: v.to(dev) for k, v in sc.items() if isinstance(v, torch.Tensor)}
+    with torch.no_grad():
+        M = transformForward(world2Camera(d["cam_positions"], d["cam_orientations"]), "-z").squeeze(1).contiguous()
+        cp = transform.affineForward(M, d["points"])
+        cn = transform.linearForward(M, d["normals"])
+        cnb = torch.where(cn[..., 2:] > 0, -cn, cn).contiguous()
+        tree = sampling.build_tree(W, H, sc["focal"], cp, cnb, d["stddevs"], K, 0.0, wl["precision"])
+    prm, ws = tree["_prm"], tree["_ws"]
+    prm.seed = 1234
+    prm.tile_x = autotune.lookup(torch.cuda.get_device_name(dev), W, H, cp.shape[1], K) or 8
+    idx = torch.full((W, H, K), -1, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def call():
+        _lib.check(L.uds_sample_descent(prm, 0, None, idx.data_ptr(), ws.data_ptr(), ws.numel(), stream.cuda_stream),
+                   "descent")
+
+    for _ in range(args.warmup):
+        call()
+    ts = []
+    for _ in range(args.steps):
+        flush.fill_(1)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        call()
+        e1.record(stream)
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    print(json.dumps({"metric": "descent kernel ms", "workload": workload_name("harmonic500k", wl),
+                      "tile_x": prm.tile_x, "steps": args.steps, "warmup": args.warmup,
+                      "ms_median": float(np.median(ts)), "visible_splats": tree["n_visible"],
+                      "coefficients": tree["n_coefs"]}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -565,9 +670,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="harmonic500k",
-                    choices=sorted(WORKLOADS) + sorted(MULTIVIEW) + ["proposal", "next"])
-    ap.add_argument("--seeds", type=int, default=8, help="proposal workload: sampling calls per method")
-    ap.add_argument("--train-steps", type=int, default=600, help="proposal workload: Adam steps")
+                    choices=sorted(WORKLOADS) + sorted(MULTIVIEW) + ["proposal", "next", "descent"])
+    ap.add_argument("--seeds", type=int, default=16, help="proposal record: sampling calls per method")
+    ap.add_argument("--train-steps", type=int, default=1000, help="proposal record: Adam steps")
+    ap.add_argument("--no-proposal", action="store_true", help="leave the learned-proposal record out")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--eager", action="store_true", help="time eager steps instead of a CUDA-graph replay")
     args = ap.parse_args()
@@ -575,6 +681,8 @@ def main():
         return proposal_main(args)
     if args.workload == "next":
         return next_rows_main(args)
+    if args.workload == "descent":
+        return descent_main(args)
     if args.workload in MULTIVIEW:
         return multiview_main(args, args.workload, MULTIVIEW[args.workload])
     wl = WORKLOADS[args.workload]
@@ -779,6 +887,24 @@ def main():
     else:
         peak, peak_src = 6800.0, "fallback"
     achieved = bytes_alg / t_desc / 1e9
+    # the issue-rate diagnostic beside the HBM fraction: warp instructions per
+    # launch (ncu) over the live kernel time at the sampled SM clock, per SM
+    # sub-partition (peak 1 instruction per cycle)
+    inst = profiled("warp_instructions_per_launch") if args.workload == "harmonic500k" else None
+    issue_rate = None
+    if inst:
+        props = torch.cuda.get_device_properties(dev)
+        mhz = clk.get("sm_mhz") or 2070.0
+        ipc = inst / (t_desc * mhz * 1e6 * props.multi_processor_count * 4)
+        issue_rate = {"warp_instructions_per_launch": inst, "ipc_per_smsp": ipc, "peak": 1.0, "frac": ipc,
+                      "sm_mhz": mhz}
+
+    prop = None
+    if rank == 0 and not args.no_proposal and args.workload == "harmonic500k":
+        try:
+            prop = proposal_record(train_steps=args.train_steps, seeds=args.seeds)
+        except Exception as e:  # the record never decides the headline
+            prop = {"failed": str(e)}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -802,11 +928,13 @@ def main():
                     "eager_value": world * S / t_e2e_eager / 1e6},
             "eager_ms_per_step": t_eager,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": profiled_traffic() if args.workload == "harmonic500k" else None,
-                         "traffic_source": "ncu capture, profiles/k_sample_harmonic500k_1024.md",
+                         "traffic": profiled("traffic_bytes_per_launch") if args.workload == "harmonic500k" else None,
+                         "traffic_source": "ncu capture of this build, profiles/k_sample_harmonic500k_1024.md",
+                         "issue_rate": issue_rate,
                          "kernel": "k_sample (per-pixel descent)",
                          "kernel_ms": t_desc * 1e3, "bytes_alg": int(bytes_alg), "peak_source": peak_src},
             "cpu_baseline": cpu,
+            "proposal": prop,
             "clocks": clk,
             "gpu_launches": int(launches),
         }), flush=True)

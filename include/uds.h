@@ -157,10 +157,14 @@ int uds_sample_proposal(const uds_sample_params* prm, const float* points, const
  * uds_tree_build in `workspace`: stochastic descents with exact FGT masses
  * from every stride-th pixel (both directions), `draws` per pixel; each
  * visited internal node appends (16 features, m_left / (m_left + m_right)) to
- * X (cap x 16) and target (cap).  *count (device int, preset to 0) receives
- * the number of rows produced (it may exceed cap; rows past cap are dropped). */
+ * X (cap x 16) and target (cap), and, when keys is not NULL, the row's key
+ * (pixel << 16 | draw << 8 | depth) to keys (cap): rows are appended in no
+ * fixed order, sorting by key gives a fixed one.  *count (device int, preset
+ * to 0) receives the number of rows produced (it may exceed cap; rows past
+ * cap are dropped). */
 int uds_proposal_dataset(const uds_sample_params* prm, int stride, int draws, float* X, float* target,
-                         int32_t* count, int cap, const void* workspace, size_t workspace_bytes, void* stream);
+                         int64_t* keys, int32_t* count, int cap, const void* workspace, size_t workspace_bytes,
+                         void* stream);
 
 /* Debug view of one tree (for tests): builds view `view` and copies the
  * first n_visible entries of each array (host-sized by the caller from
@@ -268,10 +272,14 @@ int uds_mlp_forward_tiles(int R_max, const int* R_dev, const void* X_tiles, cons
 /* Training: adds the gradient of the mean cross-entropy between
  * softmax(logits) and (target, 1 - target) over the R rows to grad (fp32,
  * uds_mlp_param_count() entries, zeroed by the caller) and the mean loss to
- * *loss (device float).  uds_mlp_adam: one Adam step (bias-corrected, step
- * >= 1) on params with moments m1, m2; consumes (zeroes) grad. */
+ * *loss (device float).  Each block's partial sums go to the workspace
+ * (uds_mlp_grad_workspace_size(R) bytes) and are added in block order, so the
+ * result is the same on every run.  uds_mlp_adam: one Adam step
+ * (bias-corrected, step >= 1) on params with moments m1, m2; consumes
+ * (zeroes) grad. */
+size_t uds_mlp_grad_workspace_size(int R);
 int uds_mlp_grad(int R, const float* X, const float* target, const float* params, float* grad, float* loss,
-                 int* err, void* stream);
+                 int* err, void* workspace, size_t workspace_bytes, void* stream);
 int uds_mlp_adam(float* params, float* grad, float* m1, float* m2, int step, float lr, float beta1, float beta2,
                  float eps, void* stream);
 

@@ -107,8 +107,9 @@ def test_mlp_grad(L, R):
     lo = torch.zeros(1, device=DEV)
     err = torch.zeros(1, dtype=torch.int32, device=DEV)
     Pd, Xd, td = P.to(DEV), X.to(DEV), target.to(DEV)
+    ws = torch.empty(L.uds_mlp_grad_workspace_size(R), dtype=torch.uint8, device=DEV)
     assert L.uds_mlp_grad(R, Xd.data_ptr(), td.data_ptr(), Pd.data_ptr(), G.data_ptr(), lo.data_ptr(),
-                          err.data_ptr(), torch.cuda.current_stream().cuda_stream) == 0
+                          err.data_ptr(), ws.data_ptr(), ws.numel(), torch.cuda.current_stream().cuda_stream) == 0
     torch.cuda.synchronize()
     assert int(err.item()) == 0
     assert abs(float(lo.item()) - float(loss.detach())) < 1e-3 * abs(float(loss.detach())) + 1e-4
@@ -135,10 +136,11 @@ def test_mlp_training_reduces_loss(L):
     err = torch.zeros(1, dtype=torch.int32, device=DEV)
     s = torch.cuda.current_stream().cuda_stream
     losses = []
+    ws = torch.empty(L.uds_mlp_grad_workspace_size(X.shape[0]), dtype=torch.uint8, device=DEV)
     for step in range(1, 301):
         lo = torch.zeros(1, device=DEV)
         assert L.uds_mlp_grad(X.shape[0], X.data_ptr(), target.data_ptr(), P.data_ptr(), G.data_ptr(), lo.data_ptr(),
-                              err.data_ptr(), s) == 0
+                              err.data_ptr(), ws.data_ptr(), ws.numel(), s) == 0
         assert L.uds_mlp_adam(P.data_ptr(), G.data_ptr(), m1.data_ptr(), m2.data_ptr(), step, 3e-3, 0.9, 0.999,
                               1e-8, s) == 0
         if step in (1, 300):

@@ -83,12 +83,25 @@ def test_weighted_estimator_unbiased(setup, learned):
     se = (var / S).sqrt()
     live = mass > 1e-2
     z = ((mean - exact).abs() / (se + 1e-3 * exact.abs() + 1e-6))[live]
-    # The network is trained with atomically summed gradients, so it (and the
-    # largest z over thousands of pixels of a heavy-tailed weighted estimate)
-    # varies from run to run; a bias would raise z over many pixels.
+    # training is deterministic (fixed row order, gradients summed in block
+    # order), so these figures are the same on every run; a bias would raise
+    # z over many pixels
+    print("z mean / q995 / max", float(z.mean()), float(torch.quantile(z, 0.995)), float(z.max()))
     assert float(z.mean()) < 1.5, float(z.mean())
     assert float(torch.quantile(z, 0.995)) < 4.5, float(torch.quantile(z, 0.995))
-    assert float(z.max()) < 8.0, float(z.max())
+    assert float(z.max()) < 6.0, float(z.max())
+
+
+def test_training_is_deterministic(setup):
+    """The same data and seeds give the same rows and the same trained
+    parameters, bit for bit."""
+    proposal = setup["proposal"]
+    X2, t2 = proposal.dataset(*setup["args"], 0.0, 1e-4, stride=2, draws=8, seed=3)
+    assert torch.equal(X2, setup["X"]) and torch.equal(t2, setup["t"])
+    net2 = proposal.ProposalNet(DEV, seed=1)
+    losses = net2.train(X2, t2, steps=400, batch=16384, lr=3e-3).cpu()
+    assert torch.equal(net2.params, setup["net"].params)
+    assert torch.equal(losses, setup["losses"])
 
 
 def test_trained_network_gains(setup):

@@ -68,7 +68,9 @@ _SIGS = {
     "uds_mma_probe": (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_void_p]),
     "uds_mlp_param_count": (c_int, []),
     "uds_mlp_forward": (c_int, [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
-    "uds_mlp_grad": (c_int, [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "uds_mlp_grad_workspace_size": (c_size_t, [c_int]),
+    "uds_mlp_grad": (c_int, [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
+                             c_void_p]),
     "uds_mlp_adam": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_float, c_float, c_float, c_float,
                              c_void_p]),
     "uds_mlp_forward_dev": (c_int, [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
@@ -77,8 +79,8 @@ _SIGS = {
     "uds_sample_proposal": (c_int, [ctypes.POINTER(SampleParams), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                     c_float, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
                                     c_void_p]),
-    "uds_proposal_dataset": (c_int, [ctypes.POINTER(SampleParams), c_int, c_int, c_void_p, c_void_p, c_void_p, c_int,
-                                     c_void_p, c_size_t, c_void_p]),
+    "uds_proposal_dataset": (c_int, [ctypes.POINTER(SampleParams), c_int, c_int, c_void_p, c_void_p, c_void_p,
+                                     c_void_p, c_int, c_void_p, c_size_t, c_void_p]),
     "uds_pixel_scatter": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p]),
     "uds_pixel_gather_workspace_size": (c_size_t, [c_int, c_int, c_int, c_int, c_int]),
     "uds_pixel_gather": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_int, c_int, c_void_p, c_void_p, c_int,

@@ -395,7 +395,7 @@ struct MlpGradSmem {
     float dz4f[mlp::kTile][2];
     float bias[3 * mlp::kHid + mlp::kOut];
     float dbias[3 * mlp::kHid + mlp::kOut];
-    float loss;
+    float wloss[4];
     uint64_t mbar;
     uint32_t taddr;
 };
@@ -424,9 +424,15 @@ __device__ __forceinline__ void stage_transposed(unsigned char* dst, const float
     }
 }
 
+// Each block writes its partial gradients (and loss) to its own slice of
+// part (kParams + 1 floats per block, every slot written by one thread);
+// k_mlp_grad_reduce then sums the slices in block order, so the gradient does
+// not depend on the order in which blocks finish.
+constexpr int kGradPart = mlp::kParams + 1;
+
 __global__ void __launch_bounds__(128) k_mlp_grad(int R, const float* __restrict__ X, const float* __restrict__ target,
-                                                  float scale, const float* __restrict__ P, float* __restrict__ G,
-                                                  float* __restrict__ loss_out, int* __restrict__ err) {
+                                                  float scale, const float* __restrict__ P,
+                                                  float* __restrict__ part, int* __restrict__ err) {
     extern __shared__ __align__(1024) unsigned char s_raw[];
     MlpGradSmem& S = *reinterpret_cast<MlpGradSmem*>(s_raw);
     using namespace mlp;
@@ -445,10 +451,7 @@ __global__ void __launch_bounds__(128) k_mlp_grad(int R, const float* __restrict
     }
     // dz4 columns 2..15 stay zero
     for (int i = tid; i < kTile * kOut * 2 / 16; i += 128) reinterpret_cast<uint4*>(S.dz4)[i] = make_uint4(0, 0, 0, 0);
-    if (tid == 0) {
-        S.loss = 0.0f;
-        tc::mbar_init(&S.mbar, 1);
-    }
+    if (tid == 0) tc::mbar_init(&S.mbar, 1);
     if (warp == 0) {
         tc::tmem_alloc(&S.taddr, 64);
         tc::tmem_relinquish();
@@ -631,27 +634,44 @@ __global__ void __launch_bounds__(128) k_mlp_grad(int R, const float* __restrict
         __syncthreads();
     }
     if (!ok && (tid & 31) == 0) atomicExch(err, 1);
-    // flush the accumulators
+    // this block's partial sums: one writer per slot, no atomics
+    float* G = part + (size_t)blockIdx.x * kGradPart;
 #pragma unroll
     for (int i = 0; i < 32; ++i) {
-        atomicAdd(&G[oW3 + go * kHid + gi + i], g3[i]);
-        atomicAdd(&G[oW2 + go * kHid + gi + i], g2[i]);
+        G[oW3 + go * kHid + gi + i] = g3[i];
+        G[oW2 + go * kHid + gi + i] = g2[i];
     }
 #pragma unroll
-    for (int i = 0; i < 8; ++i) atomicAdd(&G[oW1 + go * kIn + gi1 + i], g1[i]);
-    atomicAdd(&G[oW4 + (tid >> 6) * kHid + (tid & 63)], g4);
+    for (int i = 0; i < 8; ++i) G[oW1 + go * kIn + gi1 + i] = g1[i];
+    G[oW4 + (tid >> 6) * kHid + (tid & 63)] = g4;
     for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
-    if ((tid & 31) == 0) atomicAdd(&S.loss, lsum);
+    if ((tid & 31) == 0) S.wloss[warp] = lsum;
     tc::fence_before_sync();
     __syncthreads();
     for (int i = tid; i < kHid; i += 128) {
-        atomicAdd(&G[oB1 + i], S.dbias[i]);
-        atomicAdd(&G[oB2 + i], S.dbias[kHid + i]);
-        atomicAdd(&G[oB3 + i], S.dbias[2 * kHid + i]);
+        G[oB1 + i] = S.dbias[i];
+        G[oB2 + i] = S.dbias[kHid + i];
+        G[oB3 + i] = S.dbias[2 * kHid + i];
     }
-    if (tid < 2) atomicAdd(&G[oB4 + tid], S.dbias[3 * kHid + tid]);
-    if (tid == 0) atomicAdd(loss_out, S.loss * scale);
+    if (tid < 2) G[oB4 + tid] = S.dbias[3 * kHid + tid];
+    if (tid == 0) G[kParams] = (((S.wloss[0] + S.wloss[1]) + S.wloss[2]) + S.wloss[3]) * scale;
     if (warp == 0) tc::tmem_dealloc(taddr, 64);
+}
+
+// grad += the blocks' partial gradients summed in block order; loss += the
+// blocks' partial losses.  Slots of the zero rows of the last layer are not
+// written by the blocks and are skipped.
+__global__ void k_mlp_grad_reduce(int nb, const float* __restrict__ part, float* __restrict__ G,
+                                  float* __restrict__ loss_out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > mlp::kParams) return;
+    bool dead = i < mlp::kParams &&
+                ((i >= mlp::oW4 + 2 * mlp::kHid && i < mlp::oB4) || i >= mlp::oB4 + 2);
+    if (dead) return;
+    float s = 0.0f;
+    for (int b = 0; b < nb; ++b) s += part[(size_t)b * kGradPart + i];
+    if (i < mlp::kParams) G[i] += s;
+    else loss_out[0] += s;
 }
 
 // Adam step on the flat parameters; the gradient is consumed (zeroed).
@@ -716,24 +736,37 @@ extern "C" int uds_mlp_forward_dev(int R_max, const int* R_dev, const float* X, 
     return launch_status();
 }
 
+static int mlp_grad_blocks(int R) {
+    int tiles = (R + uds::mlp::kTile - 1) / uds::mlp::kTile;
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return tiles < sms ? tiles : sms;
+}
+
+extern "C" size_t uds_mlp_grad_workspace_size(int R) {
+    if (R <= 0) return 0;
+    return sizeof(float) * (size_t)uds::kGradPart * (size_t)mlp_grad_blocks(R);
+}
+
 extern "C" int uds_mlp_grad(int R, const float* X, const float* target, const float* params, float* grad,
-                            float* loss, int* err, void* stream) {
+                            float* loss, int* err, void* workspace, size_t workspace_bytes, void* stream) {
     using namespace uds;
     if (R < 0 || (R > 0 && (!X || !target || !params || !grad || !loss)) || !err) return UDS_ERR_ARGUMENT;
     if (R == 0) return UDS_OK;
+    if (!workspace || workspace_bytes < uds_mlp_grad_workspace_size(R)) return UDS_ERR_WORKSPACE;
     static bool attr = false;
     size_t smem = sizeof(MlpGradSmem) + 1024;
     if (!attr) {
         cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         attr = true;
     }
-    int tiles = (R + mlp::kTile - 1) / mlp::kTile;
-    int dev = 0, sms = 148;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    int grid = tiles < sms ? tiles : sms;
-    k_mlp_grad<<<grid, 128, smem, as_stream(stream)>>>(R, X, target, 1.0f / (float)R, params, grad, loss, err);
-    return launch_status();
+    int grid = mlp_grad_blocks(R);
+    float* part = reinterpret_cast<float*>(workspace);
+    cudaStream_t s = as_stream(stream);
+    k_mlp_grad<<<grid, 128, smem, s>>>(R, X, target, 1.0f / (float)R, params, part, err);
+    k_mlp_grad_reduce<<<cdiv(kGradPart, 256), 256, 0, s>>>(grid, part, grad, loss);
+    return launch_status(2);
 }
 
 extern "C" int uds_mlp_adam(float* params, float* grad, float* m1, float* m2, int step, float lr, float beta1,

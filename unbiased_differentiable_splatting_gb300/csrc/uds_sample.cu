@@ -1457,7 +1457,8 @@ __device__ __forceinline__ float draw_uniform(uint64_t seed, uint32_t pixel, uin
 __global__ void __launch_bounds__(128) k_prop_dataset(Tree T, const ViewState* vs, int W, int H, int stride,
                                                       int draws, float precision, uint64_t seed, uint32_t view,
                                                       float* __restrict__ X, float* __restrict__ target,
-                                                      int* __restrict__ count, int cap) {
+                                                      long long* __restrict__ keys, int* __restrict__ count,
+                                                      int cap) {
     int j = (blockIdx.x * blockDim.x + threadIdx.x) * stride;
     int i = (blockIdx.y * blockDim.y + threadIdx.y) * stride;
     if (i >= W || j >= H) return;
@@ -1497,6 +1498,7 @@ __global__ void __launch_bounds__(128) k_prop_dataset(Tree T, const ViewState* v
 #pragma unroll
                 for (int q = 0; q < kFeat; ++q) X[(size_t)r * kFeat + q] = f[q];
                 target[r] = pl;
+                if (keys) keys[r] = ((long long)pixel << 16) | ((long long)k << 8) | d;
             }
             v = draw_uniform(seed, pixel, view, 0xA0000000u, k, d) <= pl ? L.x : L.y;
         }
@@ -2137,17 +2139,19 @@ extern "C" int uds_sample_proposal(const uds_sample_params* prm, const float* po
 }
 
 extern "C" int uds_proposal_dataset(const uds_sample_params* prm, int stride, int draws, float* X, float* target,
-                                    int32_t* count, int cap, const void* workspace, size_t workspace_bytes,
-                                    void* stream) {
+                                    int64_t* keys, int32_t* count, int cap, const void* workspace,
+                                    size_t workspace_bytes, void* stream) {
     int st = check_params(prm);
     if (st) return st;
-    if (stride < 1 || draws < 1 || cap < 0 || !count || (cap > 0 && (!X || !target))) return UDS_ERR_ARGUMENT;
+    if (stride < 1 || draws < 1 || draws > 255 || cap < 0 || !count || (cap > 0 && (!X || !target)))
+        return UDS_ERR_ARGUMENT;
     Ws w = layout(prm, reinterpret_cast<char*>(const_cast<void*>(workspace)));
     if (!workspace || workspace_bytes < w.bytes) return UDS_ERR_WORKSPACE;
     if (prm->N == 0) return UDS_OK;
     dim3 block(16, 8);
     dim3 grid(cdiv(cdiv(prm->H, stride), block.x), cdiv(cdiv(prm->W, stride), block.y));
     k_prop_dataset<<<grid, block, 0, as_stream(stream)>>>(tree_of(w), w.vs, prm->W, prm->H, stride, draws,
-                                                          prm->precision, prm->seed, 0u, X, target, count, cap);
+                                                          prm->precision, prm->seed, 0u, X, target,
+                                                          reinterpret_cast<long long*>(keys), count, cap);
     return launch_status();
 }

@@ -17,7 +17,7 @@ from __future__ import annotations
 
 import torch
 
-from ._lib import SampleParams, Workspace, check, load, need, ptr, stream_ptr
+from ._lib import SampleParams, Workspace, check, load, need, ptr, stream_ptr  # noqa: F401
 from .cudaExtensions import sampling
 
 LAYERS = ((64, 16), (64, 64), (64, 64), (16, 64))  # (out, in); the last layer's rows 2..15 are zero
@@ -73,11 +73,13 @@ class ProposalNet:
         g = torch.Generator(device=self.device).manual_seed(seed)
         losses = torch.zeros(steps, device=self.device)
         n = X.shape[0]
+        nb = min(batch, n)
+        ws = Workspace.get(self.device, L.uds_mlp_grad_workspace_size(nb), "mlp_grad")
         for i in range(steps):
-            sel = torch.randint(0, n, (min(batch, n),), device=self.device, generator=g)
+            sel = torch.randint(0, n, (nb,), device=self.device, generator=g)
             xb, tb = X[sel].contiguous(), target[sel].contiguous()
             check(L.uds_mlp_grad(xb.shape[0], ptr(xb), ptr(tb), ptr(self.params), ptr(self.grad), ptr(losses[i:]),
-                                 ptr(self._err), s), "mlp grad")
+                                 ptr(self._err), ptr(ws), ws.numel(), s), "mlp grad")
             self.steps += 1
             check(L.uds_mlp_adam(ptr(self.params), ptr(self.grad), ptr(self.m1), ptr(self.m2), self.steps, lr, 0.9,
                                  0.999, 1e-8, s), "mlp adam")
@@ -89,19 +91,28 @@ class ProposalNet:
 
 def dataset(width, height, focallength, points, normals, stdDevs, smoothing, precision, stride=4, draws=8,
             cap=2_000_000, seed=0):
-    """(features (R,16), target (R,)) from stochastic descents on view 0."""
+    """(features (R,16), target (R,)) from stochastic descents on view 0, in
+    a fixed order (sorted by pixel, draw and depth), at most cap rows (the
+    first rows of that order when there are more)."""
     tree = sampling.build_tree(width, height, focallength, points[:1], normals[:1], stdDevs[:1], 8, smoothing,
                                precision)
     prm, ws = tree["_prm"], tree["_ws"]
     prm.seed = int(seed)
     dev = points.device
-    X = torch.empty((cap, 16), device=dev)
-    t = torch.empty(cap, device=dev)
-    count = torch.zeros(1, dtype=torch.int32, device=dev)
-    check(load().uds_proposal_dataset(prm, stride, draws, ptr(X), ptr(t), ptr(count), cap, ptr(ws), ws.numel(),
-                                      stream_ptr(dev)), "proposal dataset")
-    n = min(int(count.item()), cap)
-    return X[:n], t[:n]
+    room = cap
+    while True:
+        X = torch.empty((room, 16), device=dev)
+        t = torch.empty(room, device=dev)
+        keys = torch.empty(room, dtype=torch.int64, device=dev)
+        count = torch.zeros(1, dtype=torch.int32, device=dev)
+        check(load().uds_proposal_dataset(prm, stride, draws, ptr(X), ptr(t), ptr(keys), ptr(count), room, ptr(ws),
+                                          ws.numel(), stream_ptr(dev)), "proposal dataset")
+        n = int(count.item())
+        if n <= room:
+            break
+        room = n  # every row kept, so that the order (and the cut at cap) is fixed
+    order = torch.argsort(keys[:n])[:cap]
+    return X[order], t[order]
 
 
 def sample(width, height, focallength, points, normals, stdDevs, numSamples, smoothing, precision, net=None,
