@@ -254,11 +254,12 @@ def reference_arm(args, wl, name):
 
 def multiview_main(args, name, wl):
     """Several views (possibly of different resolutions) per step: one
-    Splatting module per resolution group, one summed L2 loss, backward to the
+    MultiViewSplatting module (one descent launch over all views' pixels, the
+    fused render pass per run of same-size views), one summed L2 loss, backward to the
     splats and the camera poses; the whole step captured as one CUDA graph."""
     import torch
     from unbiased_differentiable_splatting_gb300 import load, scenes
-    from unbiased_differentiable_splatting_gb300.render import RenderOptions, Splatting
+    from unbiased_differentiable_splatting_gb300.render import MultiViewSplatting, RenderOptions
     if args.impl == "reference":
         print(json.dumps({"impl": "reference", "unavailable": "multi-view workloads are timed for this build only; "
                           "the reference arm times the default workload"}))
@@ -291,38 +292,32 @@ def multiview_main(args, name, wl):
         pert_q, pert_t = co.clone(), cp.clone()
     d = {k: v.to(dev) for k, v in sc.items() if isinstance(v, torch.Tensor)}
     seed_t = torch.tensor([99], dtype=torch.int64, device=dev)
-    groups, v0 = [], 0
+    views = []
     for (W, H, f, nv) in wl["groups"]:
         f = f if f is not None else scenes.focal_from_fov(W)
-        opts = RenderOptions(forward="-z", numSamples=K, precision=wl["precision"], shadingMode=wl["shading"])
-        r = Splatting(opts, None, W, H, f, 0.1, 100.0, smoothing=0.0).to(dev)
-        r.sample_kwargs = {"seed": seed_t}
-        groups.append((r, slice(v0, v0 + nv), W, H))
-        v0 += nv
-    S = sum(W * H * (sl.stop - sl.start) * K for _, sl, W, H in groups)
-    # autotune the descent's warp tile per resolution group (on its first view)
+        views += [(W, H, f)] * nv
+    opts = RenderOptions(forward="-z", numSamples=K, precision=wl["precision"], shadingMode=wl["shading"])
+    r = MultiViewSplatting(opts, None, views, 0.1, 100.0, 0.0).to(dev)
+    S = sum(W * H * K for (W, H, _) in views)
+    # autotune the descent's warp tile on the largest view (the one launch
+    # over all views uses one tile shape)
     from unbiased_differentiable_splatting_gb300 import autotune
     from unbiased_differentiable_splatting_gb300.extensions import transformForward, world2Camera
     from unbiased_differentiable_splatting_gb300.cudaExtensions import transform
-    tiles = []
+    big = max(range(nviews), key=lambda b: views[b][0] * views[b][1])
     with torch.no_grad():
-        for r, sl, W, H in groups:
-            v = slice(sl.start, sl.start + 1)
-            M = transformForward(world2Camera(d["cam_positions"][v], d["cam_orientations"][v]), "-z").squeeze(1)
-            cp = transform.affineForward(M.contiguous(), d["points"])
-            cn = transform.linearForward(M.contiguous(), d["normals"])
-            cnb = torch.where(cn[..., 2:] > 0, -cn, cn).contiguous()
-            best, _ = autotune.tune_descent(W, H, r.focallength, cp, cnb, d["stddevs"], K, 0.0, wl["precision"])
-            # the cache is keyed by the view's splat count, which is N for every view
-            tiles.append(best)
+        v = slice(big, big + 1)
+        M = transformForward(world2Camera(d["cam_positions"][v], d["cam_orientations"][v]), "-z").squeeze(1)
+        cp = transform.affineForward(M.contiguous(), d["points"])
+        cn = transform.linearForward(M.contiguous(), d["normals"])
+        cnb = torch.where(cn[..., 2:] > 0, -cn, cn).contiguous()
+        W, H, f = views[big]
+        tile, _ = autotune.tune_descent(W, H, f, cp, cnb, d["stddevs"], K, 0.0, wl["precision"])
+    r.sample_kwargs = {"seed": seed_t, "tile_x": tile}
 
     def render(pos, quat, pts, nrm, sd, col):
-        out = []
-        for r, sl, W, H in groups:
-            img, _, _ = r(pos[sl], quat[sl], pts, nrm, sd, col, d["ambient"], d["lamp_directions"][sl],
-                          d["lamp_intensities"])
-            out.append(img)
-        return out
+        imgs, _, _ = r(pos, quat, pts, nrm, sd, col, d["ambient"], d["lamp_directions"], d["lamp_intensities"])
+        return imgs
 
     with torch.no_grad():
         targets = [t.detach() for t in render(d["cam_positions"], d["cam_orientations"], d["points"], d["normals"],
@@ -375,8 +370,8 @@ def multiview_main(args, name, wl):
         "metric": "fwd+bwd Msamples/s", "value": S / (t * 1e-3) / 1e6, "unit": "Msamples/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": name, "views": [f"{sl.stop - sl.start}x{W}x{H}" for _, sl, W, H in groups],
-                   "descent_tiles": tiles,
+        "config": {"workload": name, "views": [f"{nv}x{W}x{H}" for (W, H, _, nv) in wl["groups"]],
+                   "descent_tile": tile, "descent_launches_per_step": 1,
                    "samples_per_step": S, "surfels": wl["n"], "K": K, "shading": wl["shading"],
                    "l2": "flushed (256 MiB write) before each step", "cuda_graph": True},
         "loss": float(static_loss.item()), "pose_grad_finite": bool(torch.isfinite(g).all().item()) if g is not None

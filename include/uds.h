@@ -123,6 +123,25 @@ int uds_sample(const uds_sample_params* prm, const float* points, const float* n
                int32_t* indices, uds_view_stats* stats, void* workspace, size_t workspace_bytes,
                void* stream);
 
+/* Geometry of one view of an uneven batch. */
+typedef struct {
+    int32_t W, H;   /* image size */
+    float focal;    /* focal length in pixels */
+    int32_t reserved;
+} uds_view_desc;
+
+/* ---- sampling.sample for B views of different sizes in one call (no
+ *      counterpart in the reference, whose host loop runs one view at a time,
+ *      samplingCuda.cu:216-289): every view's tree built (side streams), then
+ *      one descent launch over all views' pixels for K <= 8 and B <= 32 (one
+ *      launch per view otherwise).  views: host array of B descriptors (prm's
+ *      W, H and focal are ignored); indices packed view after view, view b's
+ *      (W_b,H_b,K) block first; Philox uniforms from seed with counter view b
+ *      (no uniforms tensor).  Workspace: uds_sample_workspace_size(prm). ---- */
+int uds_sample_views(const uds_sample_params* prm, const uds_view_desc* views, const float* points,
+                     const float* normals, const float* std_devs, const float* h_override, int32_t* indices,
+                     uds_view_stats* stats, void* workspace, size_t workspace_bytes, void* stream);
+
 /* Stochastic sampling mode (no counterpart in the reference, whose sampler is
  * the deterministic Poisson descent above): each of the K draws of a pixel
  * descends from the root into a child with probability proportional to its

@@ -31,6 +31,12 @@ class SampleParams(ctypes.Structure):
                 ("fixed_degree", ctypes.c_int32)]
 
 
+class ViewDesc(ctypes.Structure):
+    """uds_view_desc (include/uds.h)."""
+
+    _fields_ = [("W", ctypes.c_int32), ("H", ctypes.c_int32), ("focal", c_float), ("reserved", ctypes.c_int32)]
+
+
 VIEW_STATS_FIELDS = ("h", "radius", "n_visible", "n_coefs", "demoted", "overflow")
 
 _SIGS = {
@@ -56,6 +62,8 @@ _SIGS = {
     "uds_sample_workspace_size": (c_size_t, [ctypes.POINTER(SampleParams)]),
     "uds_sample": (c_int, [ctypes.POINTER(SampleParams), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                            c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "uds_sample_views": (c_int, [ctypes.POINTER(SampleParams), ctypes.POINTER(ViewDesc), c_void_p, c_void_p, c_void_p,
+                                 c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "uds_sample_stochastic": (c_int, [ctypes.POINTER(SampleParams), c_void_p, c_void_p, c_void_p, c_void_p,
                                       c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "uds_tree_build": (c_int, [ctypes.POINTER(SampleParams), c_int, c_void_p, c_void_p, c_void_p, c_void_p,

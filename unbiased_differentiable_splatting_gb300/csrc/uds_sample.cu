@@ -1077,18 +1077,44 @@ __device__ void warp_root_walk(const Tree& T, float qx, float qy, bool live, Mas
     if (deep && live) total = node_weight_out_of_line(T, 0, qx, qy);
 }
 
-template <int R, int KM>
+// Views of different sizes in one descent launch: blocks [first[v],
+// first[v+1]) of the one-dimensional grid cover view v, bx[v] blocks along
+// y per block row; its indices start at entry ioff[v] of the packed output.
+constexpr int kMaxUneven = 32;
+struct UnevenViews {
+    int nv;
+    int first[kMaxUneven + 1];
+    int bx[kMaxUneven];
+    int W[kMaxUneven], H[kMaxUneven];
+    long long ioff[kMaxUneven];
+};
+
+template <int R, int KM, bool UNEVEN>
 __global__ void __launch_bounds__(128, 4) k_sample(Tree T, const ViewState* vs, int W, int H, int K,
                                                 float precision, const float* __restrict__ uniforms,
                                                 uint64_t seed, const uint64_t* __restrict__ seed_ptr,
                                                 uint32_t view, int* __restrict__ indices, uds_view_stats* st,
-                                                size_t vstride, size_t ustride, size_t istride) {
+                                                size_t vstride, size_t ustride, size_t istride, UnevenViews uv) {
     // block tile_x (y) x 128 / tile_x (x).  blockIdx.z selects the
     // view: its tree lives vstride bytes after the previous view's, its
     // uniforms ustride floats and its indices istride entries further on.
+    // With UNEVEN the view and the block's place in it come from uv
+    // (blockIdx.x only; no uniforms tensor).
     if (seed_ptr) seed = *seed_ptr;
-    if (blockIdx.z) {
-        size_t off = (size_t)blockIdx.z * vstride;
+    unsigned bxi = blockIdx.x, byi = blockIdx.y, vz = blockIdx.z;
+    if (UNEVEN) {
+        int b = 0;
+        while (b + 1 < uv.nv && uv.first[b + 1] <= (int)blockIdx.x) ++b;
+        int local = (int)blockIdx.x - uv.first[b];
+        bxi = (unsigned)(local % uv.bx[b]);
+        byi = (unsigned)(local / uv.bx[b]);
+        vz = (unsigned)b;
+        W = uv.W[b];
+        H = uv.H[b];
+        indices += uv.ioff[b];
+    }
+    if (vz) {
+        size_t off = (size_t)vz * vstride;
         T.lnk = shifted(T.lnk, off);
         T.par = shifted(T.par, off);
         T.box = shifted(T.box, off);
@@ -1097,15 +1123,17 @@ __global__ void __launch_bounds__(128, 4) k_sample(Tree T, const ViewState* vs, 
         T.leaf_xy = shifted(T.leaf_xy, off);
         T.leaf_id = shifted(T.leaf_id, off);
         vs = shifted(vs, off);
-        view += blockIdx.z;
-        indices += (size_t)blockIdx.z * istride;
-        if (uniforms) uniforms += (size_t)blockIdx.z * ustride;
-        st += blockIdx.z;
+        view += vz;
+        if (!UNEVEN) {
+            indices += (size_t)vz * istride;
+            if (uniforms) uniforms += (size_t)vz * ustride;
+        }
+        st += vz;
     }
     __shared__ WalkStack s_walk[4];
     const unsigned full = 0xffffffffu;
-    int j = blockIdx.x * blockDim.x + threadIdx.x;
-    int i = blockIdx.y * blockDim.y + threadIdx.y;
+    int j = bxi * blockDim.x + threadIdx.x;
+    int i = byi * blockDim.y + threadIdx.y;
     int tid = threadIdx.x + blockDim.x * threadIdx.y;
     int warp = tid >> 5, lane = tid & 31;
     bool live = (i < W && j < H);
@@ -1753,14 +1781,27 @@ static void launch_sample(const Tree& T, const Ws& w, const uds_sample_params* p
     dim3 grid(cdiv(p->H, block.x), cdiv(p->W, block.y), nviews);
     size_t istride = (size_t)p->W * p->H * p->K;
     size_t ustride = (size_t)p->W * p->H * R * p->K;
+    UnevenViews none{};
     if (R <= 3 && p->K <= 8)
-        k_sample<(R <= 3 ? R : 3), 8><<<grid, block, 0, s>>>(T, w.vs, p->W, p->H, p->K, p->precision, u, p->seed,
-                                                             p->seed_dev, (uint32_t)view, idx, w.stats + view,
-                                                             vstride, ustride, istride);
+        k_sample<(R <= 3 ? R : 3), 8, false><<<grid, block, 0, s>>>(T, w.vs, p->W, p->H, p->K, p->precision, u,
+                                                                    p->seed, p->seed_dev, (uint32_t)view, idx,
+                                                                    w.stats + view, vstride, ustride, istride, none);
     else
-        k_sample<(R >= 3 ? R : 3), kMaxK><<<grid, block, 0, s>>>(T, w.vs, p->W, p->H, p->K, p->precision, u,
-                                                                 p->seed, p->seed_dev, (uint32_t)view, idx,
-                                                                 w.stats + view, vstride, ustride, istride);
+        k_sample<(R >= 3 ? R : 3), kMaxK, false><<<grid, block, 0, s>>>(T, w.vs, p->W, p->H, p->K, p->precision, u,
+                                                                        p->seed, p->seed_dev, (uint32_t)view, idx,
+                                                                        w.stats + view, vstride, ustride, istride,
+                                                                        none);
+}
+
+// Views of different sizes (K <= 8) in one launch: a one-dimensional grid of
+// every view's blocks; uv built by the caller.
+template <int R>
+static void launch_sample_uneven(const Tree& T, const Ws& w, const uds_sample_params* p, const UnevenViews& uv,
+                                 int* idx, cudaStream_t s, size_t vstride) {
+    int tx = p->tile_x > 0 ? p->tile_x : 8;
+    dim3 block(tx, 128 / tx);
+    k_sample<R, 8, true><<<uv.first[uv.nv], block, 0, s>>>(T, w.vs, 0, 0, p->K, p->precision, nullptr, p->seed,
+                                                           p->seed_dev, 0u, idx, w.stats, vstride, 0, 0, uv);
 }
 
 static int check_params(const uds_sample_params* p) {
@@ -1883,6 +1924,111 @@ extern "C" int uds_sample(const uds_sample_params* prm, const float* points, con
             default: launch_sample<8>(T, w, prm, uniforms, 0, indices, s, B, slot); break;
         }
         if ((st = launch_status())) return st;
+    }
+    if (stats) {
+        e = cudaMemcpyAsync(stats, w.stats, sizeof(uds_view_stats) * prm->B, cudaMemcpyDeviceToDevice, s);
+        if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
+    }
+    return UDS_OK;
+}
+
+// Views of different sizes in one call: every view's tree in its own slot,
+// then one descent launch over all views' pixels (K <= 8; larger K, or more
+// than kMaxUneven views, one launch per view).  prm->W, H and focal are
+// replaced by each view's; indices are packed view after view.
+extern "C" int uds_sample_views(const uds_sample_params* prm, const uds_view_desc* views, const float* points,
+                                const float* normals, const float* std_devs, const float* h_override,
+                                int32_t* indices, uds_view_stats* stats, void* workspace, size_t workspace_bytes,
+                                void* stream) {
+    int st = check_params(prm);
+    if (st) return st;
+    if (!views || !indices || (prm->N > 0 && (!points || !normals || !std_devs))) return UDS_ERR_ARGUMENT;
+    size_t total = 0;
+    for (int b = 0; b < prm->B; ++b) {
+        if (views[b].W <= 0 || views[b].H <= 0 || !(views[b].focal > 0.0f)) return UDS_ERR_ARGUMENT;
+        total += (size_t)views[b].W * views[b].H * prm->K;
+    }
+    char* base = reinterpret_cast<char*>(workspace);
+    Ws w = layout(prm, base);
+    size_t slot = w.bytes;  // does not depend on the image size
+    if (!workspace || workspace_bytes < slot * (size_t)prm->B) return UDS_ERR_WORKSPACE;
+    cudaStream_t s = as_stream(stream);
+    cudaError_t e = cudaMemsetAsync(indices, 0xFF, sizeof(int32_t) * total, s);
+    if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
+    BuildStreams* bs = prm->B > 1 ? build_streams(s) : nullptr;
+    int nside = bs ? (prm->B < kBuildStreams ? prm->B : kBuildStreams) : 0;
+    std::unique_lock<std::mutex> hold;
+    if (nside) hold = std::unique_lock<std::mutex>(bs->enqueue);
+    if (nside) {
+        e = cudaEventRecord(bs->fork, s);
+        for (int k = 0; k < nside && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(bs->side[k], bs->fork, 0);
+        if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
+    }
+    for (int b = 0; b < prm->B; ++b) {
+        uds_sample_params pv = *prm;
+        pv.W = views[b].W;
+        pv.H = views[b].H;
+        pv.focal = views[b].focal;
+        Ws wb = layout(&pv, base + slot * (size_t)b);
+        wb.stats = w.stats;
+        cudaStream_t sb = nside ? bs->side[b % nside] : s;
+        if ((st = build_view(&pv, wb, b, points, normals, std_devs, h_override, sb))) return st;
+    }
+    if (nside) {
+        for (int k = 0; k < nside && e == cudaSuccess; ++k) {
+            e = cudaEventRecord(bs->join[k], bs->side[k]);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(s, bs->join[k], 0);
+        }
+        if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
+    }
+    if (prm->N > 0) {
+        Tree T = tree_of(w);
+        int R = num_rounds(prm->K);
+        int tx = prm->tile_x > 0 ? prm->tile_x : 8;
+        if (prm->K <= 8 && prm->B <= kMaxUneven) {
+            UnevenViews uv{};
+            uv.nv = prm->B;
+            long long off = 0;
+            int blocks = 0;
+            for (int b = 0; b < prm->B; ++b) {
+                uv.first[b] = blocks;
+                uv.bx[b] = (int)cdiv(views[b].H, tx);
+                uv.W[b] = views[b].W;
+                uv.H[b] = views[b].H;
+                uv.ioff[b] = off;
+                blocks += uv.bx[b] * (int)cdiv(views[b].W, 128 / tx);
+                off += (long long)views[b].W * views[b].H * prm->K;
+            }
+            uv.first[prm->B] = blocks;
+            switch (R) {
+                case 1: launch_sample_uneven<1>(T, w, prm, uv, indices, s, slot); break;
+                case 2: launch_sample_uneven<2>(T, w, prm, uv, indices, s, slot); break;
+                default: launch_sample_uneven<3>(T, w, prm, uv, indices, s, slot); break;
+            }
+            if ((st = launch_status())) return st;
+        } else {
+            size_t off = 0;
+            for (int b = 0; b < prm->B; ++b) {
+                uds_sample_params pv = *prm;
+                pv.W = views[b].W;
+                pv.H = views[b].H;
+                Ws wb = layout(&pv, base + slot * (size_t)b);
+                wb.stats = w.stats;
+                Tree Tb = tree_of(wb);
+                switch (R) {
+                    case 1: launch_sample<1>(Tb, wb, &pv, nullptr, b, indices + off, s); break;
+                    case 2: launch_sample<2>(Tb, wb, &pv, nullptr, b, indices + off, s); break;
+                    case 3: launch_sample<3>(Tb, wb, &pv, nullptr, b, indices + off, s); break;
+                    case 4: launch_sample<4>(Tb, wb, &pv, nullptr, b, indices + off, s); break;
+                    case 5: launch_sample<5>(Tb, wb, &pv, nullptr, b, indices + off, s); break;
+                    case 6: launch_sample<6>(Tb, wb, &pv, nullptr, b, indices + off, s); break;
+                    case 7: launch_sample<7>(Tb, wb, &pv, nullptr, b, indices + off, s); break;
+                    default: launch_sample<8>(Tb, wb, &pv, nullptr, b, indices + off, s); break;
+                }
+                if ((st = launch_status())) return st;
+                off += (size_t)views[b].W * views[b].H * prm->K;
+            }
+        }
     }
     if (stats) {
         e = cudaMemcpyAsync(stats, w.stats, sizeof(uds_view_stats) * prm->B, cudaMemcpyDeviceToDevice, s);

@@ -35,7 +35,7 @@ import math
 
 import torch
 
-from .._lib import SampleParams, Workspace, check, load, need, ptr, stream_ptr
+from .._lib import SampleParams, ViewDesc, Workspace, check, load, need, ptr, stream_ptr
 
 MAX_DEGREE = 16
 
@@ -126,6 +126,47 @@ def sample(width: int, height: int, focallength: float, points, normals, colors,
     if return_stats:
         return indices, view_stats(stats)
     return indices
+
+
+def sample_views(views, points, normals, colors, stdDevs, numSamples: int, smoothing: float, precision: float,
+                 seed=None, h=None, return_stats=False, max_degree=MAX_DEGREE, coef_pool=0, tile_x=None,
+                 fixed_degree=0):
+    """sampling.sample for B views of different sizes in one call (no
+    reference counterpart): ``views`` is a list of B (width, height,
+    focallength); points / normals (B,N,3), stdDevs (1|B,N,2).  Every view's
+    tree is built, then one descent launch covers all views' pixels (K <= 8).
+    Returns the list of (1, W_b, H_b, K) int32 index tensors (views of one
+    packed buffer), and the per-view stats when asked.  View b draws the
+    Philox uniforms of view b of ``sample`` on a view of that size."""
+    _check(points, normals, stdDevs)
+    dev = points.device
+    B, K = points.shape[0], int(numSamples)
+    if len(views) != B:
+        raise ValueError("one (width, height, focallength) per view of points")
+    if seed is None:
+        seed = int(torch.randint(0, 2 ** 62, (1,)).item())
+    W0, H0, f0 = views[0]
+    prm = params(W0, H0, f0, points, stdDevs, K, smoothing, precision, seed, max_degree, coef_pool,
+                 _tile(points, W0, H0, K, tile_x), fixed_degree)
+    desc = (ViewDesc * B)(*[ViewDesc(int(w), int(hh), float(f), 0) for (w, hh, f) in views])
+    if h is not None:
+        need(h, "h", device=dev)
+        if h.numel() != B:
+            raise ValueError("h must have B entries")
+    L = load()
+    ws = Workspace.get(dev, workspace_bytes(prm), "sample")
+    sizes = [int(w) * int(hh) * K for (w, hh, _) in views]
+    packed = torch.empty(sum(sizes), dtype=torch.int32, device=dev)
+    stats = torch.empty((B, 8), dtype=torch.float32, device=dev) if return_stats else None
+    check(L.uds_sample_views(prm, desc, ptr(points), ptr(normals), ptr(stdDevs), ptr(h), ptr(packed), ptr(stats),
+                             ptr(ws), ws.numel(), stream_ptr(dev)), "sampling sample_views")
+    out, o = [], 0
+    for (w, hh, _), n in zip(views, sizes):
+        out.append(packed[o:o + n].view(1, int(w), int(hh), K))
+        o += n
+    if return_stats:
+        return out, view_stats(stats)
+    return out
 
 
 def sample_stochastic(width: int, height: int, focallength: float, points, normals, stdDevs, numSamples: int,

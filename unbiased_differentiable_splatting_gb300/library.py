@@ -46,6 +46,22 @@ def _(width, height, focallength, points, normals, stdDevs, numSamples, smoothin
     return points.new_empty((points.shape[0], width, height, numSamples), dtype=torch.int32)
 
 
+@_op("uds::sample_views", mutates_args=())
+def sample_views(widths: List[int], heights: List[int], focallengths: List[float], points: Tensor, normals: Tensor,
+                 stdDevs: Tensor, numSamples: int, smoothing: float, precision: float, seed: int,
+                 seed_tensor: Optional[Tensor]) -> List[Tensor]:
+    """Views of different sizes in one call: [(1,W_b,H_b,K) int32 per view]."""
+    views = list(zip(widths, heights, focallengths))
+    out = sampling.sample_views(views, points, normals, None, stdDevs, numSamples, smoothing, precision,
+                                seed=seed_tensor if seed_tensor is not None else seed)
+    return [t.clone() for t in out]
+
+
+@sample_views.register_fake
+def _(widths, heights, focallengths, points, normals, stdDevs, numSamples, smoothing, precision, seed, seed_tensor):
+    return [points.new_empty((1, w, h, numSamples), dtype=torch.int32) for w, h in zip(widths, heights)]
+
+
 # --------------------------------------------------------------------- EWA
 @_op("uds::splat_forward", mutates_args=())
 def splat_forward(width: int, height: int, focallength: float, indices: Tensor, points: Tensor, normals: Tensor,
@@ -526,7 +542,7 @@ def _(nearest, points, normals, sigma, mean):
     return points.new_empty((2,)), torch.empty_like(points), torch.empty_like(normals)
 
 
-OPS = ("sample", "splat_forward", "splat_backward", "ewa_weights", "render_splats", "render_splats_backward", "filter_forward", "filter_backward", "interp_forward",
+OPS = ("sample", "sample_views", "splat_forward", "splat_backward", "ewa_weights", "render_splats", "render_splats_backward", "filter_forward", "filter_backward", "interp_forward",
        "interp_backward", "affine_forward", "affine_backward", "linear_forward", "linear_backward",
        "view_matrix_forward", "view_matrix_backward", "backface", "backface_backward", "shade_forward", "shade_backward", "shade_sh_forward",
        "shade_sh_backward", "lambert_forward", "lambert_backward", "pixel_scatter", "pixel_gather", "nearest",

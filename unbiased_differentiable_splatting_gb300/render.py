@@ -213,3 +213,82 @@ class Splatting(th.nn.Module):
         else:
             raise ValueError("Unkown shading mode")
         return image, indices, depthWeights
+
+
+class MultiViewSplatting(th.nn.Module):
+    """Splatting.forward for B views of different sizes in one pass (no
+    counterpart module in the reference, which renders one view size per
+    module): the transforms and back-face flips of all views at once, one
+    sampling call whose descent covers every view's pixels in one launch
+    (``sampling.sample_views``), then the fused render pass once per run of
+    consecutive views of one size.  ``views`` lists (width, height,
+    focallength) per view.  The shading modes that interpolate one per-splat
+    attribute are supported: forward, forwardHarmonics, None.
+
+    forward(...) takes Splatting.forward's arguments for all B views and
+    returns (images, indices, depthWeights): lists with one (1,W_b,H_b,.)
+    tensor per view."""
+
+    MODES = ("forward", "forwardHarmonics", "None")
+
+    def __init__(self, opts, logger, views, zmin: float, zmax: float, smoothing: float) -> None:
+        super().__init__()
+        if opts.shadingMode not in self.MODES:
+            raise ValueError(f"MultiViewSplatting interpolates per-splat attributes ({', '.join(self.MODES)}); "
+                             f"use one Splatting per view size for shading mode {opts.shadingMode!r}")
+        self.views = [(int(w), int(h), float(f)) for (w, h, f) in views]
+        self.coordForward = getattr(opts, "forward", "-z")
+        self.smoothing = float(smoothing)
+        self.numSamples = int(opts.numSamples)
+        self.precision = float(opts.precision)
+        self.shadingMode = opts.shadingMode
+        self.backface = BackfaceCulling()
+        self.forwardShading = Lambert()
+        self.forwardHarmonics = ForwardSphericalHaromic()
+        self.sample_kwargs = {}
+        # runs of consecutive views of one size: (first view, count, W, H, f)
+        self.groups = []
+        for b, v in enumerate(self.views):
+            if self.groups and self.groups[-1][2:] == v and self.groups[-1][0] + self.groups[-1][1] == b:
+                g = self.groups[-1]
+                self.groups[-1] = (g[0], g[1] + 1, *v)
+            else:
+                self.groups.append((b, 1, *v))
+
+    def forward(self, camPositions, camOrientations, pointPositions, pointNormals, pointStdDevs, pointDiffuse,
+                ambientLight, lampDirections, lampIntensities):
+        from .cudaExtensions import sampling
+        transformMatrix = world2Camera(camPositions, camOrientations)
+        transformMatrix = transformForward(transformMatrix, self.coordForward).squeeze(1).contiguous()
+        camPoints = AffineTransform.apply(transformMatrix, pointPositions)
+        camNormals = LinearTransform.apply(transformMatrix, pointNormals)
+        harmonics = self.shadingMode == "forwardHarmonics"
+        flipped, backfaceNormals = self.backface(pointNormals if harmonics else None, camNormals)
+        with th.no_grad():
+            packed = sampling.sample_views(self.views, camPoints.detach(), backfaceNormals.detach().contiguous(),
+                                           None, pointStdDevs.detach(), self.numSamples, self.smoothing,
+                                           self.precision, **self.sample_kwargs)
+        camLampDirections = LinearTransform.apply(transformMatrix, lampDirections)
+        if self.shadingMode == "forward":
+            perSplat = self.forwardShading(ambientLight, camLampDirections, lampIntensities, camNormals, pointDiffuse)
+        elif harmonics:
+            perSplat = self.forwardHarmonics(flipped, pointDiffuse)
+        else:
+            perSplat = pointDiffuse
+        B = camPoints.shape[0]
+        images, indices, depth = [], [], []
+        for (b0, nb, W, H, f) in self.groups:
+            sl = slice(b0, b0 + nb)
+            # consecutive views of one size are consecutive in the packed buffer
+            K = self.numSamples
+            idx = packed[b0].as_strided((nb, W, H, K), (W * H * K, H * K, K, 1))
+            sd = pointStdDevs if pointStdDevs.shape[0] == 1 else pointStdDevs[sl]
+            attr = perSplat if perSplat.shape[0] == 1 and B > 1 else perSplat[sl]
+            img, dw, _ = th.ops.uds.render_splats(W, H, f, idx, camPoints[sl].contiguous(),
+                                                  camNormals[sl].contiguous(), sd.contiguous(), self.smoothing,
+                                                  attr.contiguous())
+            for k in range(nb):
+                images.append(img[k:k + 1])
+                indices.append(idx[k:k + 1])
+                depth.append(dw[k:k + 1])
+        return images, indices, depth
