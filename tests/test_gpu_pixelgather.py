@@ -43,6 +43,18 @@ def test_scatter_gather(pg, hot):
     np.testing.assert_allclose(at, ref, rtol=1e-4, atol=1e-4)
 
 
+@pytest.mark.parametrize("B,W,H,K,N,hot", [(1, 512, 512, 8, 300_000, True), (3, 128, 96, 5, 5_000_000, False),
+                                            (1, 7, 5, 1, 1, False)])
+def test_deterministic_gather_large(pg, B, W, H, K, N, hot):
+    """Bit-exact against the oracle's sequential sums at sizes that take up to
+    three radix passes, with one splat holding about 70% of 2M samples."""
+    idx, _, g, _ = case(3, B=B, W=W, H=H, K=K, N=N, C=2, hot=hot)
+    ref = oracle.pixel_gather(idx, g, N)
+    ti, tg = torch.as_tensor(idx).to(DEV), torch.as_tensor(g).to(DEV)
+    det = pg.gather(ti, tg, N, deterministic=True).cpu().numpy()
+    np.testing.assert_array_equal(det, ref)
+
+
 def test_pixel_scatter_gather_autograd(pg):
     from unbiased_differentiable_splatting_gb300.extensions import PixelScatterGather
     idx, v, g, N = case(2, B=1, W=16, H=16, K=4, N=60, C=2)

@@ -9,11 +9,13 @@
 //   atomic mode: lanes of a warp that hold the same splat first combine their
 //     values (__match_any_sync + shuffles), then one atomic per group and
 //     channel; the order of additions is not fixed (like the reference).
-//   deterministic mode: the samples are bucketed per splat (counts, scan,
-//     placement), each bucket is ordered by sample offset, and one thread sums
-//     its splat's values in that order, so the result is bit-identical to a
-//     sequential sum in sample order.
+//   deterministic mode: the valid samples are compacted in sample order and
+//     stably radix-sorted by splat (so each splat's samples stay in sample
+//     order, however many there are), bucket offsets come from per-splat
+//     counts, and one thread sums its splat's values in that order: the
+//     result is bit-identical to a sequential sum in sample order.
 #include "uds_common.cuh"
+#include "uds_radix.cuh"
 #include "uds_scan.cuh"
 
 namespace uds {
@@ -67,34 +69,32 @@ __global__ void k_pixel_count(size_t S, size_t per_view, int N, const int* __res
     if (id >= 0 && id < N) atomicAdd(&count[(size_t)id + (size_t)N * (t / per_view)], 1u);
 }
 
-__global__ void k_pixel_place(size_t S, size_t per_view, int N, const int* __restrict__ idx,
-                              const unsigned* __restrict__ offs, unsigned* __restrict__ fill,
-                              unsigned* __restrict__ slots) {
+__global__ void k_pixel_flags(size_t S, int N, const int* __restrict__ idx, unsigned* __restrict__ flag) {
+    size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= S) return;
+    int id = idx[t];
+    flag[t] = (id >= 0 && id < N) ? 1u : 0u;
+}
+
+// the valid samples in sample order: (splat key, sample offset) pairs
+__global__ void k_pixel_compact(size_t S, size_t per_view, int N, const int* __restrict__ idx,
+                                const unsigned* __restrict__ pos, unsigned* __restrict__ keys,
+                                unsigned* __restrict__ samples) {
     size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= S) return;
     int id = idx[t];
     if (id < 0 || id >= N) return;
-    size_t key = (size_t)id + (size_t)N * (t / per_view);
-    unsigned p = offs[key] + atomicAdd(&fill[key], 1u);
-    slots[p] = (unsigned)t;
+    unsigned p = pos[t];
+    keys[p] = (unsigned)((size_t)id + (size_t)N * (t / per_view));
+    samples[p] = (unsigned)t;
 }
 
-// one thread per splat: order its samples (insertion sort, buckets are
-// short), then sum in that order
-__global__ void k_pixel_sum(size_t M, int C, const unsigned* __restrict__ offs, unsigned* __restrict__ slots,
+// one thread per splat sums its bucket (already in sample order)
+__global__ void k_pixel_sum(size_t M, int C, const unsigned* __restrict__ offs, const unsigned* __restrict__ slots,
                             const float* __restrict__ values, float* __restrict__ out) {
     size_t key = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (key >= M) return;
     unsigned lo = offs[key], hi = offs[key + 1];
-    for (unsigned i = lo + 1; i < hi; ++i) {
-        unsigned x = slots[i];
-        unsigned j = i;
-        while (j > lo && slots[j - 1] > x) {
-            slots[j] = slots[j - 1];
-            --j;
-        }
-        slots[j] = x;
-    }
     for (int c = 0; c < C; ++c) {
         float s = 0.0f;
         for (unsigned i = lo; i < hi; ++i) s = __fadd_rn(s, values[(size_t)slots[i] * C + c]);
@@ -115,11 +115,44 @@ extern "C" int uds_pixel_scatter(int B, int W, int H, int K, const int32_t* indi
     return launch_status();
 }
 
+// Deterministic-mode scratch: per-splat counts and offsets, sample flags and
+// positions, two (key, sample) pair buffers, the radix digit histograms and
+// their scan, and the scans' tile sums.
+struct GatherWs {
+    unsigned *count, *offs, *flag, *pos, *ka, *va, *kb, *vb, *hist, *hscan, *part;
+    size_t bytes;
+};
+
+static GatherWs gather_layout(size_t M, size_t S, char* base) {
+    auto a = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    size_t nb = cdiv(S, kSortTile), nh = 256 * nb;
+    size_t longest = S > nh ? S : nh;
+    size_t parts = scan_part_entries(longest > M ? longest : M);
+    GatherWs g{};
+    size_t off = 0;
+    auto take = [&](size_t n) {
+        unsigned* p = base ? reinterpret_cast<unsigned*>(base + off) : nullptr;
+        off += a(4 * n);
+        return p;
+    };
+    g.count = take(M);
+    g.offs = take(M + 1);
+    g.flag = take(S);
+    g.pos = take(S + 1);
+    g.ka = take(S);
+    g.va = take(S);
+    g.kb = take(S);
+    g.vb = take(S);
+    g.hist = take(nh);
+    g.hscan = take(nh + 1);
+    g.part = take(parts);
+    g.bytes = off;
+    return g;
+}
+
 extern "C" size_t uds_pixel_gather_workspace_size(int B, int W, int H, int K, int N) {
     if (B <= 0 || W <= 0 || H <= 0 || K <= 0 || N < 0) return 0;
-    size_t M = (size_t)B * N, S = (size_t)B * W * H * K;
-    auto a = [](size_t x) { return (x + 255) & ~(size_t)255; };
-    return a(4 * M) * 2 + a(4 * (M + 1)) + a(4 * S) + a(4 * scan_part_entries(M));
+    return gather_layout((size_t)B * N, (size_t)B * W * H * K, nullptr).bytes;
 }
 
 extern "C" int uds_pixel_gather(int B, int W, int H, int K, const int32_t* indices, int N, int C,
@@ -138,18 +171,30 @@ extern "C" int uds_pixel_gather(int B, int W, int H, int K, const int32_t* indic
         return launch_status();
     }
     if (!workspace || workspace_bytes < uds_pixel_gather_workspace_size(B, W, H, K, N)) return UDS_ERR_WORKSPACE;
-    auto a = [](size_t x) { return (x + 255) & ~(size_t)255; };
-    char* p = reinterpret_cast<char*>(workspace);
-    unsigned* count = reinterpret_cast<unsigned*>(p);
-    unsigned* fill = reinterpret_cast<unsigned*>(p + a(4 * M));
-    unsigned* offs = reinterpret_cast<unsigned*>(p + 2 * a(4 * M));
-    unsigned* slots = reinterpret_cast<unsigned*>(p + 2 * a(4 * M) + a(4 * (M + 1)));
-    unsigned* part = reinterpret_cast<unsigned*>(p + 2 * a(4 * M) + a(4 * (M + 1)) + a(4 * S));
-    cudaError_t e = cudaMemsetAsync(count, 0, 2 * a(4 * M), s);  // count and fill
+    GatherWs g = gather_layout(M, S, reinterpret_cast<char*>(workspace));
+    cudaError_t e = cudaMemsetAsync(g.count, 0, 4 * M, s);
     if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
-    k_pixel_count<<<cdiv(S, 256), 256, 0, s>>>(S, per_view, N, indices, count);
-    exclusive_scan(M, count, offs, part, s);
-    k_pixel_place<<<cdiv(S, 256), 256, 0, s>>>(S, per_view, N, indices, offs, fill, slots);
-    k_pixel_sum<<<cdiv(M, 128), 128, 0, s>>>(M, C, offs, slots, values, out);
-    return launch_status(6);
+    // bucket offsets from the per-splat counts
+    k_pixel_count<<<cdiv(S, 256), 256, 0, s>>>(S, per_view, N, indices, g.count);
+    exclusive_scan(M, g.count, g.offs, g.part, s);
+    // valid samples in sample order, then a stable sort by splat; the number
+    // of valid samples (g.pos[S]) stays on the device
+    k_pixel_flags<<<cdiv(S, 256), 256, 0, s>>>(S, N, indices, g.flag);
+    exclusive_scan(S, g.flag, g.pos, g.part, s);
+    k_pixel_compact<<<cdiv(S, 256), 256, 0, s>>>(S, per_view, N, indices, g.pos, g.ka, g.va);
+    int bits = 1;
+    while (bits < 32 && (M - 1) >> bits) ++bits;
+    unsigned nb = cdiv(S, kSortTile);
+    unsigned *ki = g.ka, *vi = g.va, *ko = g.kb, *vo = g.vb;
+    int launched = 9;
+    for (int shift = 0; shift < bits; shift += 8) {
+        k_radix_hist<<<nb, kSortThreads, 0, s>>>((int)S, g.pos + S, ki, shift, g.hist);
+        exclusive_scan((size_t)256 * nb, g.hist, g.hscan, g.part, s);
+        k_radix_scatter<<<nb, kSortThreads, 0, s>>>((int)S, g.pos + S, ki, vi, ko, vo, shift, g.hscan);
+        unsigned* t = ki; ki = ko; ko = t;
+        t = vi; vi = vo; vo = t;
+        launched += 5;
+    }
+    k_pixel_sum<<<cdiv(M, 128), 128, 0, s>>>(M, C, g.offs, vi, values, out);
+    return launch_status(launched + 1);
 }

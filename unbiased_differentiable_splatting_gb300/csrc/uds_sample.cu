@@ -31,12 +31,12 @@
 #include <cuda_bf16.h>
 
 #include "uds_ewa.cuh"
+#include "uds_radix.cuh"
 #include "uds_tc.cuh"
 
 namespace uds {
 
 constexpr unsigned kCulledKey = 0x40000000u;  // above every 30-bit Morton key
-constexpr int kSortThreads = 256, kSortItems = 8, kSortTile = kSortThreads * kSortItems;
 constexpr int kScanThreads = 256, kScanItems = 4, kScanTile = kScanThreads * kScanItems;
 
 struct ViewState {            // per-view device scalars (lives in the workspace)
@@ -233,23 +233,6 @@ __global__ void k_cull_morton(int N, float W, float H, float f, const float* __r
 }
 
 // ---------------------------------------------------------- 3 radix sort
-// Tile of 2048 items per block: warp w owns items [w*256, w*256+256) of the
-// tile, lane l holds item w*256 + r*32 + l in round r, so (round, lane) order
-// is item order and per-warp running counts give a stable rank.
-__global__ void k_radix_hist(int N, const uint32_t* __restrict__ keys, int shift,
-                             uint32_t* __restrict__ hist) {
-    __shared__ unsigned cnt[256];
-    for (int d = threadIdx.x; d < 256; d += blockDim.x) cnt[d] = 0;
-    __syncthreads();
-    size_t base = (size_t)blockIdx.x * kSortTile;
-    for (int r = 0; r < kSortItems; ++r) {
-        size_t i = base + (size_t)r * kSortThreads + threadIdx.x;
-        if (i < (size_t)N) atomicAdd(&cnt[(keys[i] >> shift) & 255u], 1u);
-    }
-    __syncthreads();
-    for (int d = threadIdx.x; d < 256; d += blockDim.x) hist[(size_t)d * gridDim.x + blockIdx.x] = cnt[d];
-}
-
 // Exclusive scan of hist (digit-major, 256 * nb entries) in one block.
 __global__ void k_radix_scan(uint32_t* hist, int total) {
     __shared__ uint32_t part[1024];
@@ -271,56 +254,6 @@ __global__ void k_radix_scan(uint32_t* hist, int total) {
         uint32_t v = hist[i];
         hist[i] = run;
         run += v;
-    }
-}
-
-__global__ void k_radix_scatter(int N, const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
-                                uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, int shift,
-                                const uint32_t* __restrict__ hist) {
-    __shared__ unsigned wcnt[kSortThreads / 32][256];
-    __shared__ unsigned goff[256];
-    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int d = lane; d < 256; d += 32) wcnt[warp][d] = 0;
-    for (int d = threadIdx.x; d < 256; d += blockDim.x) goff[d] = hist[(size_t)d * gridDim.x + blockIdx.x];
-    __syncwarp();
-    size_t base = (size_t)blockIdx.x * kSortTile + (size_t)warp * 256;
-    uint32_t key[kSortItems], val[kSortItems];
-    unsigned rank[kSortItems];
-    unsigned lt = (1u << lane) - 1u;
-#pragma unroll
-    for (int r = 0; r < kSortItems; ++r) {
-        size_t i = base + (size_t)r * 32 + lane;
-        bool ok = i < (size_t)N;
-        key[r] = ok ? kin[i] : 0xFFFFFFFFu;
-        val[r] = ok ? vin[i] : 0u;
-        unsigned dig = ok ? ((key[r] >> shift) & 255u) : 256u;
-        unsigned peers = __match_any_sync(0xffffffffu, dig);
-        unsigned before = 0;
-        if (ok) before = wcnt[warp][dig];
-        rank[r] = before + __popc(peers & lt);
-        __syncwarp();
-        if (ok && (peers & lt) == 0) wcnt[warp][dig] = before + __popc(peers);
-        __syncwarp();
-    }
-    __syncthreads();
-    if (threadIdx.x < 256) {
-        unsigned run = 0;
-        for (int w = 0; w < kSortThreads / 32; ++w) {
-            unsigned c = wcnt[w][threadIdx.x];
-            wcnt[w][threadIdx.x] = run;
-            run += c;
-        }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int r = 0; r < kSortItems; ++r) {
-        size_t i = base + (size_t)r * 32 + lane;
-        if (i < (size_t)N) {
-            unsigned dig = (key[r] >> shift) & 255u;
-            unsigned pos = goff[dig] + wcnt[warp][dig] + rank[r];
-            kout[pos] = key[r];
-            vout[pos] = val[r];
-        }
     }
 }
 
@@ -1713,7 +1646,7 @@ static int build_view(const uds_sample_params* p, const Ws& w, int view, const f
     uint32_t *ki = w.keysA, *vi = w.idsA, *ko = w.keysB, *vo = w.idsB;
     for (int pass = 0; pass < 4; ++pass) {
         int shift = 8 * pass;
-        k_radix_hist<<<nb, kSortThreads, 0, s>>>(N, ki, shift, w.hist);
+        k_radix_hist<<<nb, kSortThreads, 0, s>>>(N, nullptr, ki, shift, w.hist);
         int nh = (int)(256 * nb);
         int launched = 3;
         if (nh <= 16 * 1024) {
@@ -1725,7 +1658,7 @@ static int build_view(const uds_sample_params* p, const Ws& w, int view, const f
             k_scan_down<<<hb, kScanThreads, 0, s>>>(w.hist, nullptr, 0, nh, w.scanTmp, w.hist);
             launched = 5;
         }
-        k_radix_scatter<<<nb, kSortThreads, 0, s>>>(N, ki, vi, ko, vo, shift, w.hist);
+        k_radix_scatter<<<nb, kSortThreads, 0, s>>>(N, nullptr, ki, vi, ko, vo, shift, w.hist);
         if ((st = launch_status(launched))) return st;
         uint32_t* t = ki; ki = ko; ko = t;
         t = vi; vi = vo; vo = t;
