@@ -50,8 +50,9 @@ MULTIVIEW = {
     # gradients for the splats and the 6-DoF poses
     "room16": dict(n=2_000_000, K=8, precision=0.01, shading="forward", groups=[(640, 480, 525.0, 16)]),
     # 300k surfels with 8 N(0,1) feature channels (no shading), views of four
-    # resolutions: 8 x 256^2, 4 x 128^2, 4 x 512^2, 4 x 1024x768 (60 deg fov)
-    "features20": dict(n=300_000, K=8, precision=0.01, shading="None",
+    # resolutions: 8 x 256^2, 4 x 128^2, 4 x 512^2, 4 x 1024x768 (60 deg fov); the
+    # autotuner sweeps the descent tile x leaf size
+    "features20": dict(n=300_000, K=8, precision=0.01, shading="None", tune_leaf=True,
                        groups=[(256, 256, None, 8), (128, 128, None, 4), (512, 512, None, 4), (1024, 768, None, 4)]),
 }
 
@@ -300,7 +301,9 @@ def multiview_main(args, name, wl):
     r = MultiViewSplatting(opts, None, views, 0.1, 100.0, 0.0).to(dev)
     S = sum(W * H * K for (W, H, _) in views)
     # autotune the descent's warp tile on the largest view (the one launch
-    # over all views uses one tile shape)
+    # over all views uses one tile shape); the uneven-batch workload sweeps
+    # tile x leaf size (a leaf size above K changes the sampled indices: each
+    # round stops at the first node holding at most that many splats)
     from unbiased_differentiable_splatting_gb300 import autotune
     from unbiased_differentiable_splatting_gb300.extensions import transformForward, world2Camera
     from unbiased_differentiable_splatting_gb300.cudaExtensions import transform
@@ -312,8 +315,13 @@ def multiview_main(args, name, wl):
         cn = transform.linearForward(M.contiguous(), d["normals"])
         cnb = torch.where(cn[..., 2:] > 0, -cn, cn).contiguous()
         W, H, f = views[big]
-        tile, _ = autotune.tune_descent(W, H, f, cp, cnb, d["stddevs"], K, 0.0, wl["precision"])
-    r.sample_kwargs = {"seed": seed_t, "tile_x": tile}
+        if wl.get("tune_leaf"):
+            (tile, leaf), tuned = autotune.tune_descent(W, H, f, cp, cnb, d["stddevs"], K, 0.0, wl["precision"],
+                                                        leaf_sizes=autotune.LEAF_CANDIDATES)
+        else:
+            tile, tuned = autotune.tune_descent(W, H, f, cp, cnb, d["stddevs"], K, 0.0, wl["precision"])
+            leaf = 0
+    r.sample_kwargs = {"seed": seed_t, "tile_x": tile, "leaf_size": leaf}
 
     def render(pos, quat, pts, nrm, sd, col):
         imgs, _, _ = r(pos, quat, pts, nrm, sd, col, d["ambient"], d["lamp_directions"], d["lamp_intensities"])
@@ -371,7 +379,8 @@ def multiview_main(args, name, wl):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": name, "views": [f"{nv}x{W}x{H}" for (W, H, _, nv) in wl["groups"]],
-                   "descent_tile": tile, "descent_launches_per_step": 1,
+                   "descent_tile": tile, "leaf_size": leaf if leaf > K else "single-splat leaves (reference rule)",
+                   "autotune_ms": {str(k): round(v, 4) for k, v in tuned.items()}, "descent_launches_per_step": 1,
                    "samples_per_step": S, "surfels": wl["n"], "K": K, "shading": wl["shading"],
                    "l2": "flushed (256 MiB write) before each step", "cuda_graph": True},
         "loss": float(static_loss.item()), "pose_grad_finite": bool(torch.isfinite(g).all().item()) if g is not None

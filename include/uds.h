@@ -80,6 +80,15 @@ typedef struct {
                                 its children's, evaluated where the adaptive
                                 error bound holds at a degree <= P; needs
                                 (N-1)(P+1)^2 floats of coefficient pool */
+    int32_t leaf_size;       /* Poisson descent only.  <= K (0: default): the
+                                reference's single-splat leaves, the descent
+                                stops at the first node holding <= K splats.
+                                K < L <= 64 (no counterpart in the reference):
+                                leaf buckets of L splats, the maximal subtrees
+                                with <= L leaves; a round stops at the first
+                                node holding <= L splats and order-samples
+                                over all of them with their exact Gaussians.
+                                A uniforms tensor is then (B,W,H,R,max(K,L)) */
 } uds_sample_params;
 
 /* ---- transform (transform.cpp:33-86: affineForward/Backward,
@@ -113,8 +122,9 @@ int uds_backface_backward(int B, int N, const float* cam_normals, const float* g
 
 /* ---- sampling.sample (sampling.cpp:48-94): points, normals (B,N,3)
  *      camera space, stdDevs (std_batch,N,2) -> indices (B,W,H,K) int32,
- *      -1 where no sample.  uniforms: optional (B,W,H,R,K) float32 in (0,1],
- *      R = ceil(sqrt(K)); NULL draws Philox4x32-10 uniforms from seed.
+ *      -1 where no sample.  uniforms: optional (B,W,H,R,M) float32 in (0,1],
+ *      R = ceil(sqrt(K)), M = max(K, leaf_size); NULL draws Philox4x32-10
+ *      uniforms from seed.
  *      h_override: optional device float[B]; entries > 0 replace the
  *      computed bandwidth.  stats: device uds_view_stats[B] (may be NULL). ---- */
 size_t uds_sample_workspace_size(const uds_sample_params* prm);

@@ -369,26 +369,29 @@ class Tree:
             raise RuntimeError("oracle sampler trace overflow")
         return ids[:m], p[:m]
 
-    def sample(self, W, H, K, precision, uniforms=None, seed=0, view=0, x0=0, x1=None, flavour=None):
+    def sample(self, W, H, K, precision, uniforms=None, seed=0, view=0, x0=0, x1=None, flavour=None, leaf_size=0):
+        """Poisson descent: indices (W,H,K).  ``leaf_size`` > K: rounds stop at
+        the first node holding <= leaf_size splats (uniforms then
+        (W,H,R,max(K,leaf_size)))."""
         idx = np.full((W, H, K), -1, np.int32)
         u = None if uniforms is None else _f(uniforms)
         fl = self.flavour if flavour is None else flavour
-        st = lib().orc_tree_sample(ctypes.c_void_p(self.ptr), C(W), C(H), C(K), F(precision), P(u),
-                                   ctypes.c_uint64(seed), ctypes.c_uint32(view), C(x0), C(W if x1 is None else x1),
-                                   C(fl), P(idx))
+        st = lib().orc_tree_sample_leaf(ctypes.c_void_p(self.ptr), C(W), C(H), C(K), C(leaf_size), F(precision), P(u),
+                                        ctypes.c_uint64(seed), ctypes.c_uint32(view), C(x0),
+                                        C(W if x1 is None else x1), C(fl), P(idx))
         if st != 0:
-            raise RuntimeError("oracle sampler trace overflow")
+            raise RuntimeError("oracle sampler trace overflow" if st == -1 else "oracle sampler: leaf size > 64")
         return idx
 
 
-def sample_fp64(tree, W, H, K, precision, seed=0, view=0, x0=0, x1=None):
+def sample_fp64(tree, W, H, K, precision, seed=0, view=0, x0=0, x1=None, leaf_size=0):
     """The estimator evaluated directly in FP64 on an oracle Tree (direct Gauss
     sums instead of Hermite expansions; same descent and order sampling with
     Philox uniforms): indices (W,H,K)."""
     idx = np.full((W, H, K), -1, np.int32)
-    st = lib().orc_tree_sample_fp64(ctypes.c_void_p(tree.ptr), C(W), C(H), C(K), ctypes.c_double(precision),
-                                    ctypes.c_uint64(seed), ctypes.c_uint32(view), C(x0), C(W if x1 is None else x1),
-                                    P(idx))
+    st = lib().orc_tree_sample_fp64_leaf(ctypes.c_void_p(tree.ptr), C(W), C(H), C(K), C(leaf_size),
+                                         ctypes.c_double(precision), ctypes.c_uint64(seed), ctypes.c_uint32(view),
+                                         C(x0), C(W if x1 is None else x1), P(idx))
     if st != 0:
         raise RuntimeError("oracle FP64 sampler: path deeper than 64 levels")
     return idx

@@ -1290,10 +1290,17 @@ static void insert_sample(int index, float key, int* indices, float* keys, int K
 /* sequentialPoissonKernel (sequentialPoissonDynamicTree.cuh:56-196) with the
  * per-pixel capacity map held as the traces of the earlier rounds (a node
  * only ever appears at its own depth), which is the hash map of
- * sampleRadixTree.cuh:29-88 without its overflow. */
-int orc_tree_sample(const orc_tree* t, int W, int H, int K, float precision, const float* uniforms,
-                    uint64_t seed, uint32_t view, int x0, int x1, int fl, int* indices) {
+ * sampleRadixTree.cuh:29-88 without its overflow.
+ * Leaf size (no reference counterpart): a round descends while its node
+ * holds more than M = max(K, leaf) splats and then order-samples over all of
+ * the node's splats; leaf <= K is the reference's rule (M = K).  The round's
+ * uniforms are M per round: uniforms[(pixel * R + r) * M + k], or Philox
+ * blocks r * ceil(M / 4) + k / 4. */
+int orc_tree_sample_leaf(const orc_tree* t, int W, int H, int K, int leaf, float precision, const float* uniforms,
+                         uint64_t seed, uint32_t view, int x0, int x1, int fl, int* indices) {
     int R = orc_num_rounds(K);
+    int M = leaf > K ? leaf : K;
+    if (M > 64) return -2;
     int n = t->n;
     int status = 0;
     if (x1 > W) x1 = W;
@@ -1313,11 +1320,11 @@ int orc_tree_sample(const orc_tree* t, int W, int H, int K, float precision, con
             float total = fmaxf(0.0f, orc_tree_node_weight(t, 0, q, fl));
             if (total < precision) continue;
             for (int r = 0; r < R && r < 8; ++r) {
-                if (uniforms) memcpy(u, &uniforms[((size_t)pixel * R + r) * K], sizeof(float) * K);
-                else orc_philox_uniforms(seed, view, (uint32_t)pixel, (uint32_t)r, K, u);
+                if (uniforms) memcpy(u, &uniforms[((size_t)pixel * R + r) * M], sizeof(float) * M);
+                else orc_philox_uniforms(seed, view, (uint32_t)pixel, (uint32_t)r, M, u);
                 int v = 0, d = 0;
                 tnode[r][0] = 0; tprob[r][0] = 1.0f;
-                while (t->count[v] > K) {
+                while (t->count[v] > M) {
                     int a = t->left[v], b = t->right[v];
                     float w0 = fmaxf(0.0f, orc_tree_node_weight(t, a, q, fl));
                     float w1 = fmaxf(0.0f, orc_tree_node_weight(t, b, q, fl));
@@ -1357,6 +1364,11 @@ int orc_tree_sample(const orc_tree* t, int W, int H, int K, float precision, con
     return status;
 }
 
+int orc_tree_sample(const orc_tree* t, int W, int H, int K, float precision, const float* uniforms,
+                    uint64_t seed, uint32_t view, int x0, int x1, int fl, int* indices) {
+    return orc_tree_sample_leaf(t, W, H, K, 0, precision, uniforms, seed, view, x0, x1, fl, indices);
+}
+
 /* The same estimator evaluated directly in FP64 (the CPU baseline the
  * reference lacks): node masses are sums of exp(-|q - y|^2 / (2 h^2)) over
  * the node's leaves in double, skipping subtrees whose box misses the
@@ -1388,9 +1400,11 @@ static double direct_trunc64(const orc_tree* t, int node, const double* q) {
     return s;
 }
 
-int orc_tree_sample_fp64(const orc_tree* t, int W, int H, int K, double precision, uint64_t seed, uint32_t view,
-                         int x0, int x1, int* indices) {
+int orc_tree_sample_fp64_leaf(const orc_tree* t, int W, int H, int K, int leaf, double precision, uint64_t seed,
+                              uint32_t view, int x0, int x1, int* indices) {
     int R = orc_num_rounds(K);
+    int M = leaf > K ? leaf : K;
+    if (M > 64) return -2;
     int n = t->n;
     int status = 0;
     if (x1 > W) x1 = W;
@@ -1409,10 +1423,10 @@ int orc_tree_sample_fp64(const orc_tree* t, int W, int H, int K, double precisio
             double q[2] = {(double)i, (double)j};
             if (direct_trunc64(t, 0, q) < precision) continue;
             for (int r = 0; r < R && r < 8; ++r) {
-                orc_philox_uniforms(seed, view, (uint32_t)pixel, (uint32_t)r, K, u);
+                orc_philox_uniforms(seed, view, (uint32_t)pixel, (uint32_t)r, M, u);
                 int v = 0, d = 0;
                 tnode[r][0] = 0; tprob[r][0] = 1.0;
-                while (t->count[v] > K) {
+                while (t->count[v] > M) {
                     int a = t->left[v], b = t->right[v];
                     double w0 = direct_trunc64(t, a, q), w1 = direct_trunc64(t, b, q);
                     double sum = w0 + w1;
@@ -1456,6 +1470,11 @@ int orc_tree_sample_fp64(const orc_tree* t, int W, int H, int K, double precisio
         }
     }
     return status;
+}
+
+int orc_tree_sample_fp64(const orc_tree* t, int W, int H, int K, double precision, uint64_t seed, uint32_t view,
+                         int x0, int x1, int* indices) {
+    return orc_tree_sample_fp64_leaf(t, W, H, K, 0, precision, seed, view, x0, x1, indices);
 }
 
 /* Stochastic mode (no reference counterpart): each of the K draws of a

@@ -138,11 +138,17 @@ double orc_tree_direct_weight(const orc_tree* t, int node, const double* query);
  * indices is the full W*H*K array.  Returns 0, or -1 on trace overflow. */
 int orc_tree_sample(const orc_tree* t, int W, int H, int K, float precision, const float* uniforms,
                     uint64_t seed, uint32_t view, int x0, int x1, int flavour, int* indices);
+/* the same with leaf buckets: a round stops at the first node holding at
+ * most max(K, leaf) splats (leaf <= K: orc_tree_sample); -2 if that is > 64 */
+int orc_tree_sample_leaf(const orc_tree* t, int W, int H, int K, int leaf, float precision, const float* uniforms,
+                         uint64_t seed, uint32_t view, int x0, int x1, int fl, int* indices);
 /* the same estimator with direct FP64 Gauss sums for the node masses (no
  * Hermite expansion; the truncation circles are kept) and FP64 descent
  * arithmetic: the CPU baseline of the whole view */
 int orc_tree_sample_fp64(const orc_tree* t, int W, int H, int K, double precision, uint64_t seed, uint32_t view,
                          int x0, int x1, int* indices);
+int orc_tree_sample_fp64_leaf(const orc_tree* t, int W, int H, int K, int leaf, double precision, uint64_t seed,
+                              uint32_t view, int x0, int x1, int* indices);
 
 /* Stochastic mode: K independent mass-proportional descents per pixel;
  * indices (W*H*K) and path probabilities probs (W*H*K). */

@@ -173,6 +173,40 @@ def test_sample_edge_cases(smp):
     _sample_both(smp, pts[None], nrm[None], sd[None], W, H, f, 8)
 
 
+@pytest.mark.parametrize("L,K", [(16, 8), (32, 8), (64, 4), (24, 13)])
+def test_sample_leaf_size_bit_exact(smp, L, K):
+    """Leaf buckets: each round stops at the first node holding <= L splats
+    and order-samples over all of them.  Indices equal the oracle's rule,
+    with a (B,W,H,R,L) uniforms tensor and with Philox uniforms, in the
+    one-view and the uneven multi-view launch; L <= K is the default rule."""
+    rng = np.random.default_rng(90 + L + K)
+    W, H, f, N = 48, 40, 40.0, 3000
+    pts, nrm, sd = camera_scene(rng, N, W, H, f, sd=(0.01, 0.03))
+    R, M = oracle.num_rounds(K), max(K, L)
+    u = rng.uniform(2.0 ** -24, 1.0, size=(1, W, H, R, M)).astype(np.float32)
+    args = (W, H, f, T(pts[None]), T(nrm[None]), T(np.zeros((1, N, 3))), T(sd[None]), K, 0.0, 0.01)
+    for kw in (dict(uniforms=T(u)), dict(seed=77)):
+        idx, st = smp.sample(*args, leaf_size=L, return_stats=True, **kw)
+        h = float(st["h"][0])
+        tree = oracle.Tree(W, H, f, pts, h, oracle.cull_radius(h, 0.01), 0.01)
+        ref = tree.sample(W, H, K, 0.01, uniforms=u[0].reshape(W * H, R, M) if "uniforms" in kw else None,
+                          seed=kw.get("seed", 0), leaf_size=L)
+        got = idx.cpu().numpy()[0]
+        assert (got >= 0).any()
+        np.testing.assert_array_equal(got, ref)
+    # the same rule in the uneven launch: view 1 is a smaller view of the same splats
+    if K <= 8:
+        views = [(W, H, f), (32, 24, 0.6 * f)]
+        out = smp.sample_views(views, T(np.stack([pts, pts])), T(np.stack([nrm, nrm])), None, T(sd[None]), K, 0.0,
+                               0.01, seed=78, leaf_size=L, return_stats=True)
+        for b, (w_, h_, f_) in enumerate(views):
+            hb = float(out[1]["h"][b])
+            tree = oracle.Tree(w_, h_, f_, pts, hb, oracle.cull_radius(hb, 0.01), 0.01)
+            np.testing.assert_array_equal(out[0][b].cpu().numpy()[0],
+                                          tree.sample(w_, h_, K, 0.01, seed=78, view=b, leaf_size=L))
+    assert torch.equal(smp.sample(*args, seed=5, leaf_size=K), smp.sample(*args, seed=5))
+
+
 def test_sample_bad_args(smp):
     x = T(np.zeros((1, 4, 3), np.float32))
     s = T(np.zeros((1, 4, 2), np.float32))
@@ -180,6 +214,11 @@ def test_sample_bad_args(smp):
         smp.sample(8, 8, 8.0, x, x, x, s, 65, 0.0, 0.01)  # K above 64
     with pytest.raises(ValueError):
         smp.sample(8, 8, 8.0, x, x, x, T(np.zeros((2, 4, 2), np.float32)), 4, 0.0, 0.01)
+    with pytest.raises((RuntimeError, ValueError)):
+        smp.sample(8, 8, 8.0, x, x, x, s, 4, 0.0, 0.01, leaf_size=65)  # leaf size above 64
+    with pytest.raises(ValueError):  # uniforms sized for K, not for the leaf size
+        smp.sample(8, 8, 8.0, x, x, x, s, 4, 0.0, 0.01, leaf_size=16,
+                   uniforms=T(np.full((1, 8, 8, 2, 4), 0.5, np.float32)))
 
 
 @pytest.mark.parametrize("K", [1, 8, 24])

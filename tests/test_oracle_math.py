@@ -148,6 +148,30 @@ def test_det_and_libm_sample_agree():
     assert (a != b).any(-1).mean() < 0.02
 
 
+def test_leaf_size_rule():
+    """Leaf sizes up to K are the reference's rule; larger leaf buckets give
+    another valid sample (and the FP64 direct evaluation of the same rule
+    mostly agrees with the FGT one)."""
+    rng = np.random.default_rng(12)
+    W, H, f, N, K = 40, 36, 34.0, 2500, 8
+    pts, nrm, sd = _scene(rng, N, W, H, f, sd=(0.01, 0.03))
+    h = oracle.view_bandwidth(W, H, f, pts, nrm, sd, 0.0)
+    t = oracle.Tree(W, H, f, pts, h, oracle.cull_radius(h, 0.01), 0.01)
+    base = t.sample(W, H, K, 0.01, seed=3)
+    for L in (0, 4, 8):
+        np.testing.assert_array_equal(t.sample(W, H, K, 0.01, seed=3, leaf_size=L), base)
+        np.testing.assert_array_equal(oracle.sample_fp64(t, W, H, K, 0.01, seed=3, leaf_size=L),
+                                      oracle.sample_fp64(t, W, H, K, 0.01, seed=3))
+    big = t.sample(W, H, K, 0.01, seed=3, leaf_size=32)
+    assert big.min() >= -1 and big.max() < N
+    assert ((big >= 0).any(-1) == (base >= 0).any(-1)).mean() > 0.99  # about the same pixels get samples
+    assert (big != base).any()
+    f64 = oracle.sample_fp64(t, W, H, K, 0.01, seed=3, leaf_size=32)
+    assert (f64 == big).all(-1).mean() > 0.8  # 0.93 at the default rule, 0.86 here: FP32 vs FP64 keys
+    with pytest.raises(RuntimeError):
+        t.sample(W, H, K, 0.01, seed=3, leaf_size=65)
+
+
 def _inclusion_probabilities(p, K, grid=20000):
     """Exact inclusion probability of each entry in the K smallest of
     X_j = U_j / p_j, U_j ~ U(0,1] independent: integrate the density of X_j

@@ -11,6 +11,12 @@ CUDA events and stores the fastest in a JSON cache keyed by (GPU name, W, H,
 N, K); ``lookup`` is what ``cudaExtensions.sampling.sample`` consults when no
 ``tile_x`` is given.  The cache file is ``$UDS_AUTOTUNE_CACHE`` or
 ``~/.cache/uds_gb300/autotune.json``.
+
+With ``leaf_sizes`` the sweep covers tile x leaf size.  The leaf size does
+change the sampled indices (``uds_sample_params.leaf_size``: a round stops at
+the first node holding at most max(K, L) splats), so its choice is kept in a
+separate cache entry that only ``sampling.sample(leaf_size="auto")`` reads
+(``lookup_leaf``); the default sampling keeps the reference's rule.
 """
 from __future__ import annotations
 
@@ -19,6 +25,7 @@ import os
 import threading
 
 CANDIDATES = (4, 8, 16, 32)
+LEAF_CANDIDATES = (0, 16, 32)
 DEFAULT_TILE = 8
 
 _lock = threading.Lock()
@@ -59,11 +66,24 @@ def lookup(device_name: str, W: int, H: int, N: int, K: int):
     return int(e["tile_x"]) if e else None
 
 
-def record(device_name: str, W: int, H: int, N: int, K: int, tile_x: int, timings_ms: dict) -> None:
+def lookup_leaf(device_name: str, W: int, H: int, N: int, K: int):
+    """Cached (tile_x, leaf_size) of a tile x leaf sweep for this shape, or
+    None."""
+    with _lock:
+        e = _load().get(key(device_name, W, H, N, K) + "|leaf")
+    return (int(e["tile_x"]), int(e["leaf_size"])) if e else None
+
+
+def record(device_name: str, W: int, H: int, N: int, K: int, tile_x: int, timings_ms: dict,
+           leaf_size=None) -> None:
     with _lock:
         c = _load()
-        c[key(device_name, W, H, N, K)] = {"tile_x": int(tile_x),
-                                           "ms": {str(k): float(v) for k, v in timings_ms.items()}}
+        entry = {"tile_x": int(tile_x), "ms": {str(k): float(v) for k, v in timings_ms.items()}}
+        k = key(device_name, W, H, N, K)
+        if leaf_size is not None:
+            entry["leaf_size"] = int(leaf_size)
+            k += "|leaf"
+        c[k] = entry
         path = cache_path()
         os.makedirs(os.path.dirname(path), exist_ok=True)
         tmp = path + f".tmp{os.getpid()}"
@@ -78,10 +98,14 @@ def choose(timings_ms: dict) -> int:
 
 
 def tune_descent(width, height, focallength, points, normals, stdDevs, numSamples, smoothing, precision,
-                 view=0, reps=3, candidates=CANDIDATES, timer=None, save=True):
+                 view=0, reps=3, candidates=CANDIDATES, timer=None, save=True, leaf_sizes=None):
     """Time the descent of view `view` for each candidate tile width and cache
     the fastest.  `timer(tile_x) -> ms` replaces the GPU timing (tests).
-    Returns (best tile_x, {tile_x: ms})."""
+    Returns (best tile_x, {tile_x: ms}).
+
+    With `leaf_sizes` (e.g. LEAF_CANDIDATES) every (tile_x, leaf_size) pair is
+    timed, `timer(tile_x, leaf_size)`, and the fastest pair is cached for
+    ``lookup_leaf``; returns ((tile_x, leaf_size), {"tile/leaf": ms})."""
     import torch
     from ._lib import check, load, stream_ptr
     from .cudaExtensions import sampling
@@ -96,8 +120,9 @@ def tune_descent(width, height, focallength, points, normals, stdDevs, numSample
         idx = torch.empty((W, H, K), dtype=torch.int32, device=dev)
         stream = torch.cuda.current_stream(dev)
 
-        def timer(tx):
+        def timer(tx, leaf=0):
             prm.tile_x = tx
+            prm.leaf_size = leaf
             ts = []
             for r in range(reps + 1):
                 e0 = torch.cuda.Event(enable_timing=True)
@@ -110,6 +135,13 @@ def tune_descent(width, height, focallength, points, normals, stdDevs, numSample
                 if r:
                     ts.append(e0.elapsed_time(e1))
             return min(ts)
+    if leaf_sizes is not None:
+        pairs = {(int(t), int(lf)): float(timer(int(t), int(lf))) for t in candidates for lf in leaf_sizes}
+        tb, lb = min(sorted(pairs), key=lambda q: pairs[q])
+        timings = {f"{t}/{lf}": v for (t, lf), v in pairs.items()}
+        if save:
+            record(name, W, H, N, K, tb, timings, leaf_size=lb)
+        return (tb, lb), timings
     timings = {int(t): float(timer(int(t))) for t in candidates}
     best = choose(timings)
     if save:

@@ -17,6 +17,7 @@ int launch_status(int launches = 1);  // UDS_OK or UDS_ERR_LAUNCH after `launche
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
 constexpr int kMaxK = 64;        // samples per pixel supported by the sampler
+constexpr int kMaxLeaf = 64;     // largest leaf size of the Poisson descent
 constexpr int kMaxRounds = 8;    // ceil(sqrt(64))
 constexpr int kTrace = 64;       // descent trace entries (reference STACKSIZE)
 constexpr int kMaxDegree = 16;   // reference MAXDEGREE

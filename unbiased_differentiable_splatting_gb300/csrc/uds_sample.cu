@@ -1024,7 +1024,7 @@ struct UnevenViews {
 
 template <int R, int KM, bool UNEVEN>
 __global__ void __launch_bounds__(128, 4) k_sample(Tree T, const ViewState* vs, int W, int H, int K,
-                                                float precision, const float* __restrict__ uniforms,
+                                                int M, float precision, const float* __restrict__ uniforms,
                                                 uint64_t seed, const uint64_t* __restrict__ seed_ptr,
                                                 uint32_t view, int* __restrict__ indices, uds_view_stats* st,
                                                 size_t vstride, size_t ustride, size_t istride, UnevenViews uv) {
@@ -1110,7 +1110,7 @@ __global__ void __launch_bounds__(128, 4) k_sample(Tree T, const ViewState* vs, 
         unsigned long long cur = 0ull;                        // this round's choice bits so far
         tp[0] = 1.0f;
         int4 L = T.lnk[0];
-        bool going = act && L.w > K;
+        bool going = act && L.w > M;
         while (__any_sync(full, going)) {
             int a = L.x, b = L.y;
             float w0 = 0.0f, w1 = 0.0f;
@@ -1173,7 +1173,7 @@ __global__ void __launch_bounds__(128, 4) k_sample(Tree T, const ViewState* vs, 
                     if (s0 < s1) { cur |= 1ull << (d - 1); tp[d] = w1; v = b; rc = rb; }
                     else { tp[d] = w0; v = a; rc = ra; }
                     L = T.lnk[v];
-                    going = L.w > K;
+                    going = L.w > M;
                 }
             }
         }
@@ -1194,35 +1194,40 @@ __global__ void __launch_bounds__(128, 4) k_sample(Tree T, const ViewState* vs, 
         }
         // order sampling over the subtree's leaves (insertSample,
         // sequentialPoissonRadixTree.cuh:15-41); a leaf's mass is its own
-        // Gaussian (degree 0, coefficient 1)
+        // Gaussian (degree 0, coefficient 1).  The subtree holds at most M
+        // leaves: K, or the leaf size when that is larger.
         int f0 = L.z, cnt = L.w;
         // the round's uniforms, drawn as the leaves use them (after the
         // descent, so they hold no registers there): Philox block
-        // (pixel, view, r * ceil(K / 4) + k / 4), or the caller's tensor
-        const float* up = uniforms ? uniforms + ((size_t)pixel * R + r) * K : nullptr;
-        const int G = (K + 3) >> 2;
+        // (pixel, view, r * ceil(M / 4) + k / 4), or the caller's tensor
+        const float* up = uniforms ? uniforms + ((size_t)pixel * R + r) * M : nullptr;
+        const int G = (M + 3) >> 2;
         uint32_t c4[4];
+#pragma unroll 1
+        for (int k0 = 0; k0 < cnt; k0 += 4) {
+            if (!up) {
+                c4[0] = (uint32_t)pixel; c4[1] = view; c4[2] = (uint32_t)(r * G + (k0 >> 2)); c4[3] = 0u;
+                philox4x32_10(c4, (uint32_t)seed, (uint32_t)(seed >> 32));
+            }
+#pragma unroll
+            for (int k4 = 0; k4 < 4; ++k4) {
+                int k = k0 + k4;
+                if (k < cnt) {
+                    float uk = up ? up[k] : bits_to_uniform(c4[k4]);
+                    int leafNode = T.n - 1 + f0 + k;
+                    float pw = fmaxf(0.0f, leaf_mass(T, T.cen[leafNode], qx, qy));
+                    float key = fdiv(uk, pw);
+                    int index = T.leaf_id[f0 + k];
+                    bool done = false;
 #pragma unroll UK
-        for (int k = 0; k < KM; ++k) {
-            if (k < cnt) {
-                if (!up && (k & 3) == 0) {
-                    c4[0] = (uint32_t)pixel; c4[1] = view; c4[2] = (uint32_t)(r * G + (k >> 2)); c4[3] = 0u;
-                    philox4x32_10(c4, (uint32_t)seed, (uint32_t)(seed >> 32));
-                }
-                float uk = up ? up[k] : bits_to_uniform(c4[k & 3]);
-                int leafNode = T.n - 1 + f0 + k;
-                float pw = fmaxf(0.0f, leaf_mass(T, T.cen[leafNode], qx, qy));
-                float key = fdiv(uk, pw);
-                int index = T.leaf_id[f0 + k];
-                bool done = false;
-#pragma unroll UK
-                for (int q = 0; q < KM; ++q) {
-                    if (!done && q < K) {
-                        if (key < keys[q]) {
-                            int ti = ids[q]; ids[q] = index; index = ti;
-                            float tk = keys[q]; keys[q] = key; key = tk;
+                    for (int q = 0; q < KM; ++q) {
+                        if (!done && q < K) {
+                            if (key < keys[q]) {
+                                int ti = ids[q]; ids[q] = index; index = ti;
+                                float tk = keys[q]; keys[q] = key; key = tk;
+                            }
+                            if (index == -1) done = true;
                         }
-                        if (index == -1) done = true;
                     }
                 }
             }
@@ -1694,6 +1699,10 @@ static int build_view(const uds_sample_params* p, const Ws& w, int view, const f
     return launch_status(6);
 }
 
+// Leaves one order-sampling round considers: the descent stops at the first
+// node holding at most max(K, leaf_size) splats.
+static int candidates(const uds_sample_params* p) { return p->leaf_size > p->K ? p->leaf_size : p->K; }
+
 static Tree tree_of(const Ws& w) {
     Tree T;
     T.lnk = w.lnk; T.par = w.par; T.box = w.box; T.cen = w.cen; T.coef = w.coef;
@@ -1713,14 +1722,16 @@ static void launch_sample(const Tree& T, const Ws& w, const uds_sample_params* p
     dim3 block(tx, 128 / tx);
     dim3 grid(cdiv(p->H, block.x), cdiv(p->W, block.y), nviews);
     size_t istride = (size_t)p->W * p->H * p->K;
-    size_t ustride = (size_t)p->W * p->H * R * p->K;
+    const int M = candidates(p);
+    size_t ustride = (size_t)p->W * p->H * R * M;
     UnevenViews none{};
     if (R <= 3 && p->K <= 8)
-        k_sample<(R <= 3 ? R : 3), 8, false><<<grid, block, 0, s>>>(T, w.vs, p->W, p->H, p->K, p->precision, u,
+        k_sample<(R <= 3 ? R : 3), 8, false><<<grid, block, 0, s>>>(T, w.vs, p->W, p->H, p->K, M, p->precision, u,
                                                                     p->seed, p->seed_dev, (uint32_t)view, idx,
                                                                     w.stats + view, vstride, ustride, istride, none);
     else
-        k_sample<(R >= 3 ? R : 3), kMaxK, false><<<grid, block, 0, s>>>(T, w.vs, p->W, p->H, p->K, p->precision, u,
+        k_sample<(R >= 3 ? R : 3), kMaxK, false><<<grid, block, 0, s>>>(T, w.vs, p->W, p->H, p->K, M, p->precision,
+                                                                        u,
                                                                         p->seed, p->seed_dev, (uint32_t)view, idx,
                                                                         w.stats + view, vstride, ustride, istride,
                                                                         none);
@@ -1733,7 +1744,8 @@ static void launch_sample_uneven(const Tree& T, const Ws& w, const uds_sample_pa
                                  int* idx, cudaStream_t s, size_t vstride) {
     int tx = p->tile_x > 0 ? p->tile_x : 8;
     dim3 block(tx, 128 / tx);
-    k_sample<R, 8, true><<<uv.first[uv.nv], block, 0, s>>>(T, w.vs, 0, 0, p->K, p->precision, nullptr, p->seed,
+    k_sample<R, 8, true><<<uv.first[uv.nv], block, 0, s>>>(T, w.vs, 0, 0, p->K, candidates(p), p->precision,
+                                                           nullptr, p->seed,
                                                            p->seed_dev, 0u, idx, w.stats, vstride, 0, 0, uv);
 }
 
@@ -1746,6 +1758,7 @@ static int check_params(const uds_sample_params* p) {
     if ((size_t)p->N * 2 >= (1u << 31)) return UDS_ERR_ARGUMENT;
     if (p->tile_x != 0 && p->tile_x != 4 && p->tile_x != 8 && p->tile_x != 16 && p->tile_x != 32)
         return UDS_ERR_ARGUMENT;
+    if (p->leaf_size < 0 || p->leaf_size > kMaxLeaf) return UDS_ERR_ARGUMENT;
     if (p->fixed_degree != 0) {
         if (p->fixed_degree != 4 && p->fixed_degree != 6 && p->fixed_degree != 8) return UDS_ERR_ARGUMENT;
         int64_t need = (int64_t)(p->N > 1 ? p->N - 1 : 0) * (p->fixed_degree + 1) * (p->fixed_degree + 1);

@@ -20,6 +20,15 @@ end so existing calls keep working:
 * ``tile_x``: width of the descent's 32-pixel warp tiles (4, 8, 16, 32);
   default: the autotuner's cached choice for this shape (see ``autotune``),
   else 8.  The indices do not depend on it.
+* ``leaf_size``: 0 or <= K (default): the reference's single-splat leaves.
+  K < L <= 64 (no reference counterpart): leaf buckets of L splats; each round
+  of the descent stops at the first node holding <= L splats and
+  order-samples over all of them with their exact Gaussians, so fewer
+  levels are descended below the expansion frontier.  The indices differ
+  from the default's (the oracle has the same rule); ``uniforms`` is then
+  (B,W,H,R,L).  ``"auto"``: the (tile, leaf size) pair the autotuner's
+  tile x leaf sweep cached for this shape (``autotune.lookup_leaf``), else
+  the default rule.
 * ``return_stats``: also return the per-view record (h, cull radius, visible
   splats, stored coefficients, demoted nodes, trace overflows) as a (B,8)
   tensor viewed from uds_view_stats.
@@ -45,14 +54,15 @@ def num_rounds(K: int) -> int:
 
 
 def params(width, height, focallength, points, stdDevs, numSamples, smoothing, precision, seed=0,
-           max_degree=MAX_DEGREE, coef_pool=0, tile_x=0, fixed_degree=0) -> SampleParams:
+           max_degree=MAX_DEGREE, coef_pool=0, tile_x=0, fixed_degree=0, leaf_size=0) -> SampleParams:
     """``seed``: an int, or a one-element int64 CUDA tensor whose value the
     kernels read when they run (a captured CUDA graph then draws new numbers
     after the tensor is updated)."""
     prm = SampleParams(B=points.shape[0], N=points.shape[1], W=int(width), H=int(height), K=int(numSamples),
                        focal=float(focallength), smoothing=float(smoothing), precision=float(precision),
                        max_degree=int(max_degree), std_batch=stdDevs.shape[0], coef_pool=int(coef_pool or 0),
-                       seed=0, seed_dev=None, tile_x=int(tile_x or 0), fixed_degree=int(fixed_degree or 0))
+                       seed=0, seed_dev=None, tile_x=int(tile_x or 0), fixed_degree=int(fixed_degree or 0),
+                       leaf_size=int(leaf_size or 0))
     if isinstance(seed, torch.Tensor):
         if seed.dtype != torch.int64 or seed.numel() != 1 or seed.device != points.device:
             raise ValueError("a seed tensor must be one int64 element on the points' device")
@@ -80,18 +90,33 @@ def _check(points, normals, stdDevs):
         raise ValueError("stdDevs must be (1|B,N,2)")
 
 
+def _device_name(dev):
+    name = _device_names.get(dev.index)
+    if name is None:
+        name = _device_names[dev.index] = torch.cuda.get_device_name(dev)
+    return name
+
+
 def _tile(points, width, height, numSamples, tile_x):
     """Descent tile width: the given one, else the autotuner's cached choice
     for this shape, else the default."""
     if tile_x:
         return int(tile_x)
     from .. import autotune
-    dev = points.device
-    name = _device_names.get(dev.index)
-    if name is None:
-        name = _device_names[dev.index] = torch.cuda.get_device_name(dev)
-    t = autotune.lookup(name, width, height, points.shape[1], numSamples)
+    t = autotune.lookup(_device_name(points.device), width, height, points.shape[1], numSamples)
     return t or autotune.DEFAULT_TILE
+
+
+def _leaf(points, width, height, numSamples, tile_x, leaf_size):
+    """(tile_x, leaf_size) with ``leaf_size="auto"`` resolved from the
+    autotuner's tile x leaf sweep."""
+    if leaf_size != "auto":
+        return _tile(points, width, height, numSamples, tile_x), int(leaf_size or 0)
+    from .. import autotune
+    e = autotune.lookup_leaf(_device_name(points.device), width, height, points.shape[1], numSamples)
+    if e is None:
+        return _tile(points, width, height, numSamples, tile_x), 0
+    return (int(tile_x) if tile_x else e[0]), e[1]
 
 
 _device_names = {}
@@ -99,20 +124,21 @@ _device_names = {}
 
 def sample(width: int, height: int, focallength: float, points, normals, colors, stdDevs, numSamples: int,
            smoothing: float, precision: float, uniforms=None, seed=None, h=None, return_stats=False,
-           max_degree=MAX_DEGREE, coef_pool=0, tile_x=None, fixed_degree=0):
+           max_degree=MAX_DEGREE, coef_pool=0, tile_x=None, fixed_degree=0, leaf_size=0):
     _check(points, normals, stdDevs)
     dev = points.device
     B = points.shape[0]
     K = int(numSamples)
     if seed is None:
         seed = int(torch.randint(0, 2 ** 62, (1,)).item())
+    tile_x, leaf_size = _leaf(points, width, height, K, tile_x, leaf_size)
     prm = params(width, height, focallength, points, stdDevs, K, smoothing, precision, seed, max_degree, coef_pool,
-                 _tile(points, width, height, K, tile_x), fixed_degree)
+                 tile_x, fixed_degree, leaf_size)
     if uniforms is not None:
         need(uniforms, "uniforms", device=dev)
-        R = num_rounds(K)
-        if tuple(uniforms.shape) != (B, int(width), int(height), R, K):
-            raise ValueError(f"uniforms must be (B,W,H,{R},{K})")
+        R, M = num_rounds(K), max(K, int(leaf_size or 0))
+        if tuple(uniforms.shape) != (B, int(width), int(height), R, M):
+            raise ValueError(f"uniforms must be (B,W,H,{R},{M})")
     if h is not None:
         need(h, "h", device=dev)
         if h.numel() != B:
@@ -130,7 +156,7 @@ def sample(width: int, height: int, focallength: float, points, normals, colors,
 
 def sample_views(views, points, normals, colors, stdDevs, numSamples: int, smoothing: float, precision: float,
                  seed=None, h=None, return_stats=False, max_degree=MAX_DEGREE, coef_pool=0, tile_x=None,
-                 fixed_degree=0):
+                 fixed_degree=0, leaf_size=0):
     """sampling.sample for B views of different sizes in one call (no
     reference counterpart): ``views`` is a list of B (width, height,
     focallength); points / normals (B,N,3), stdDevs (1|B,N,2).  Every view's
@@ -146,8 +172,9 @@ def sample_views(views, points, normals, colors, stdDevs, numSamples: int, smoot
     if seed is None:
         seed = int(torch.randint(0, 2 ** 62, (1,)).item())
     W0, H0, f0 = views[0]
-    prm = params(W0, H0, f0, points, stdDevs, K, smoothing, precision, seed, max_degree, coef_pool,
-                 _tile(points, W0, H0, K, tile_x), fixed_degree)
+    tile_x, leaf_size = _leaf(points, W0, H0, K, tile_x, leaf_size)
+    prm = params(W0, H0, f0, points, stdDevs, K, smoothing, precision, seed, max_degree, coef_pool, tile_x,
+                 fixed_degree, leaf_size)
     desc = (ViewDesc * B)(*[ViewDesc(int(w), int(hh), float(f), 0) for (w, hh, f) in views])
     if h is not None:
         need(h, "h", device=dev)

@@ -78,15 +78,15 @@ def conditionalNormalization(dx: th.Tensor, radius=1.0, eps=1e-4) -> th.Tensor:
 # --------------------------------------------------------------- sampling
 class FmmSampling:
     """extensions/__init__.py:106-117.  Calls ``torch.ops.uds.sample`` when the
-    keyword arguments are at most ``seed`` and ``uniforms``; the additions the
-    op schema leaves out (``h``, ``return_stats``, ``tile_x``, ...) go to
-    ``cudaExtensions.sampling.sample`` directly."""
+    keyword arguments are at most ``seed``, ``uniforms`` and ``leaf_size``;
+    the additions the op schema leaves out (``h``, ``return_stats``,
+    ``tile_x``, ...) go to ``cudaExtensions.sampling.sample`` directly."""
 
     @th.no_grad()
     def __call__(self, width: int, height: int, focallength: float, points: th.Tensor, normals: th.Tensor,
                  colors: th.Tensor, stdDevs: th.Tensor, numSamples: int, smoothing: float,
                  precision: float = 0.001, **kwargs) -> th.Tensor:
-        if set(kwargs) <= {"seed", "uniforms"}:
+        if set(kwargs) <= {"seed", "uniforms", "leaf_size"}:
             seed = kwargs.get("seed")
             if seed is None:
                 seed = int(th.randint(0, 2 ** 62, (1,)).item())
@@ -96,7 +96,8 @@ class FmmSampling:
                 seed = seed - (1 << 64) if seed >= (1 << 63) else seed
             return ops.sample(int(width), int(height), float(focallength), points, normals, stdDevs, int(numSamples),
                               float(smoothing), float(precision), 0 if tensor_seed else int(seed),
-                              seed if tensor_seed else None, kwargs.get("uniforms"))
+                              seed if tensor_seed else None, kwargs.get("uniforms"),
+                              int(kwargs.get("leaf_size") or 0))
         return sampling.sample(width, height, focallength, points, normals, colors, stdDevs, numSamples, smoothing,
                                precision, **kwargs)
 

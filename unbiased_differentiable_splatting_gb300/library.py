@@ -32,33 +32,36 @@ _op = torch.library.custom_op
 @_op("uds::sample", mutates_args=())
 def sample(width: int, height: int, focallength: float, points: Tensor, normals: Tensor, stdDevs: Tensor,
            numSamples: int, smoothing: float, precision: float, seed: int, seed_tensor: Optional[Tensor],
-           uniforms: Optional[Tensor]) -> Tensor:
+           uniforms: Optional[Tensor], leaf_size: int = 0) -> Tensor:
     """sampling.sample: (B,W,H,K) int32 splat indices.  The Philox key is
     ``seed_tensor`` (one int64 on the device, read when the kernels run) when
-    given, else ``seed``; ``uniforms`` (B,W,H,R,K) replaces the generator."""
+    given, else ``seed``; ``uniforms`` (B,W,H,R,max(K,leaf_size)) replaces the
+    generator."""
     return sampling.sample(width, height, focallength, points, normals, None, stdDevs, numSamples, smoothing,
-                           precision, uniforms=uniforms, seed=seed_tensor if seed_tensor is not None else seed)
+                           precision, uniforms=uniforms, seed=seed_tensor if seed_tensor is not None else seed,
+                           leaf_size=leaf_size)
 
 
 @sample.register_fake
 def _(width, height, focallength, points, normals, stdDevs, numSamples, smoothing, precision, seed, seed_tensor,
-      uniforms):
+      uniforms, leaf_size=0):
     return points.new_empty((points.shape[0], width, height, numSamples), dtype=torch.int32)
 
 
 @_op("uds::sample_views", mutates_args=())
 def sample_views(widths: List[int], heights: List[int], focallengths: List[float], points: Tensor, normals: Tensor,
                  stdDevs: Tensor, numSamples: int, smoothing: float, precision: float, seed: int,
-                 seed_tensor: Optional[Tensor]) -> List[Tensor]:
+                 seed_tensor: Optional[Tensor], leaf_size: int = 0) -> List[Tensor]:
     """Views of different sizes in one call: [(1,W_b,H_b,K) int32 per view]."""
     views = list(zip(widths, heights, focallengths))
     out = sampling.sample_views(views, points, normals, None, stdDevs, numSamples, smoothing, precision,
-                                seed=seed_tensor if seed_tensor is not None else seed)
+                                seed=seed_tensor if seed_tensor is not None else seed, leaf_size=leaf_size)
     return [t.clone() for t in out]
 
 
 @sample_views.register_fake
-def _(widths, heights, focallengths, points, normals, stdDevs, numSamples, smoothing, precision, seed, seed_tensor):
+def _(widths, heights, focallengths, points, normals, stdDevs, numSamples, smoothing, precision, seed, seed_tensor,
+      leaf_size=0):
     return [points.new_empty((1, w, h, numSamples), dtype=torch.int32) for w, h in zip(widths, heights)]
 
 
