@@ -60,20 +60,15 @@ __global__ void k_pixel_gather_atomic(size_t S, size_t per_view, int N, int C, c
     }
 }
 
-// deterministic mode
+// deterministic mode: per-splat counts and the valid-sample flags in one pass
 __global__ void k_pixel_count(size_t S, size_t per_view, int N, const int* __restrict__ idx,
-                              unsigned* __restrict__ count) {
+                              unsigned* __restrict__ count, unsigned* __restrict__ flag) {
     size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= S) return;
     int id = idx[t];
-    if (id >= 0 && id < N) atomicAdd(&count[(size_t)id + (size_t)N * (t / per_view)], 1u);
-}
-
-__global__ void k_pixel_flags(size_t S, int N, const int* __restrict__ idx, unsigned* __restrict__ flag) {
-    size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= S) return;
-    int id = idx[t];
-    flag[t] = (id >= 0 && id < N) ? 1u : 0u;
+    bool ok = id >= 0 && id < N;
+    flag[t] = ok ? 1u : 0u;
+    if (ok) atomicAdd(&count[(size_t)id + (size_t)N * (t / per_view)], 1u);
 }
 
 // the valid samples in sample order: (splat key, sample offset) pairs
@@ -174,19 +169,18 @@ extern "C" int uds_pixel_gather(int B, int W, int H, int K, const int32_t* indic
     GatherWs g = gather_layout(M, S, reinterpret_cast<char*>(workspace));
     cudaError_t e = cudaMemsetAsync(g.count, 0, 4 * M, s);
     if (e != cudaSuccess) { set_last_error(e); return UDS_ERR_CUDA; }
-    // bucket offsets from the per-splat counts
-    k_pixel_count<<<cdiv(S, 256), 256, 0, s>>>(S, per_view, N, indices, g.count);
+    // bucket offsets from the per-splat counts; the valid samples in sample
+    // order, then a stable sort by splat; the number of valid samples
+    // (g.pos[S]) stays on the device
+    k_pixel_count<<<cdiv(S, 256), 256, 0, s>>>(S, per_view, N, indices, g.count, g.flag);
     exclusive_scan(M, g.count, g.offs, g.part, s);
-    // valid samples in sample order, then a stable sort by splat; the number
-    // of valid samples (g.pos[S]) stays on the device
-    k_pixel_flags<<<cdiv(S, 256), 256, 0, s>>>(S, N, indices, g.flag);
     exclusive_scan(S, g.flag, g.pos, g.part, s);
     k_pixel_compact<<<cdiv(S, 256), 256, 0, s>>>(S, per_view, N, indices, g.pos, g.ka, g.va);
     int bits = 1;
     while (bits < 32 && (M - 1) >> bits) ++bits;
     unsigned nb = cdiv(S, kSortTile);
     unsigned *ki = g.ka, *vi = g.va, *ko = g.kb, *vo = g.vb;
-    int launched = 9;
+    int launched = 8;
     for (int shift = 0; shift < bits; shift += 8) {
         k_radix_hist<<<nb, kSortThreads, 0, s>>>((int)S, g.pos + S, ki, shift, g.hist);
         exclusive_scan((size_t)256 * nb, g.hist, g.hscan, g.part, s);
