@@ -1010,6 +1010,41 @@ __device__ void warp_root_walk(const Tree& T, float qx, float qy, bool live, Mas
     if (deep && live) total = node_weight_out_of_line(T, 0, qx, qy);
 }
 
+// Child masses (w0, w1) = getWeight of the children (a, b) for every lane
+// of the warp with `need` (all lanes call this together).  The 2c
+// evaluations of the c lanes that need them are spread over the warp's 32
+// lanes, evaluation e being the child e % 2 of the (e / 2)-th needing lane
+// (in lane order), so a lane waits for one series instead of two while c <=
+// 16; the value of each is the same node_weight call whichever lane makes
+// it.  `owner`: 32 ints of the warp's shared memory.
+__device__ __forceinline__ void warp_child_masses(const Tree& T, bool need, int a, int b, float qx, float qy,
+                                                  float& w0, float& w1, int* owner) {
+    const unsigned full = 0xffffffffu;
+    unsigned nm = __ballot_sync(full, need);
+    if (!nm) return;
+    const int lane = (threadIdx.x + blockDim.x * threadIdx.y) & 31;
+    int c2 = 2 * __popc(nm);
+    int rank = __popc(nm & ((1u << lane) - 1u));
+    if (need) owner[rank] = lane;
+    __syncwarp();
+#pragma unroll 1
+    for (int e0 = 0; e0 < c2; e0 += 32) {
+        int e = e0 + lane;
+        int o = e < c2 ? owner[e >> 1] : lane;
+        float oqx = __shfl_sync(full, qx, o), oqy = __shfl_sync(full, qy, o);
+        int oa = __shfl_sync(full, a, o), ob = __shfl_sync(full, b, o);
+        float x = 0.0f;
+        if (e < c2) x = fmaxf(0.0f, node_weight(T, (e & 1) ? ob : oa, oqx, oqy));
+        int src = 2 * rank - e0;  // the lane holding this lane's first child in this pass
+        float x0 = __shfl_sync(full, x, src & 31), x1 = __shfl_sync(full, x, (src + 1) & 31);
+        if (need && src >= 0 && src < 32) {
+            w0 = x0;
+            w1 = x1;
+        }
+    }
+    __syncwarp();  // owner is rewritten by the next call
+}
+
 // Views of different sizes in one descent launch: blocks [first[v],
 // first[v+1]) of the one-dimensional grid cover view v, bx[v] blocks along
 // y per block row; its indices start at entry ioff[v] of the packed output.
@@ -1079,6 +1114,7 @@ __global__ void __launch_bounds__(128, 4) k_sample(Tree T, const ViewState* vs, 
     MassCache mc;
     float total;
     warp_root_walk(T, qx, qy, live, mc, total, s_walk[warp]);
+    int* ws_owner = s_walk[warp].right;  // free once the walk is done
     total = fmaxf(0.0f, total);
     bool act = live && !(total < precision);
     if (!__any_sync(full, act)) return;
@@ -1128,18 +1164,12 @@ __global__ void __launch_bounds__(128, 4) k_sample(Tree T, const ViewState* vs, 
                     need = true;
                 }
             }
-            // every lane that needs its node's child masses evaluates them
-            // at once, whatever node it is at (below the expansion frontier a
-            // child is one expansion, so the divergence is only in the
+            // every lane that needs its node's child masses gets them in the
+            // same pass, whatever node it is at (below the expansion frontier
+            // a child is one expansion, so the divergence is only in the
             // series' trip counts); one call site keeps the walk inlined once,
             // small enough for the instruction cache
-            if (need) {
-#pragma unroll 1
-                for (int ch = 0; ch < 2; ++ch) {
-                    float x = fmaxf(0.0f, node_weight(T, ch ? b : a, qx, qy));
-                    if (ch) w1 = x; else w0 = x;
-                }
-            }
+            warp_child_masses(T, need, a, b, qx, qy, w0, w1, ws_owner);
             if (going) {
                 // (re)write unconditionally: a hit stores the same masses, and
                 // a store does not wait on the per-thread memory like a load
@@ -1316,15 +1346,9 @@ __global__ void __launch_bounds__(128, 4) k_stochastic(Tree T, const ViewState* 
                     need = true;
                 }
             }
-            // every lane that needs its node's child masses evaluates them
-            // at once (one call site: the walk is inlined once)
-            if (need) {
-#pragma unroll 1
-                for (int ch = 0; ch < 2; ++ch) {
-                    float x = fmaxf(0.0f, node_weight(T, ch ? b : a, qx, qy));
-                    if (ch) w1 = x; else w0 = x;
-                }
-            }
+            // every lane that needs its node's child masses gets them in the
+            // same pass (one call site: the walk is inlined once)
+            warp_child_masses(T, need, a, b, qx, qy, w0, w1, s_walk[warp].right);
             if (going) {
                 cv[d] = v;
                 cw0[d] = w0;
