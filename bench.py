@@ -300,28 +300,24 @@ def multiview_main(args, name, wl):
     opts = RenderOptions(forward="-z", numSamples=K, precision=wl["precision"], shadingMode=wl["shading"])
     r = MultiViewSplatting(opts, None, views, 0.1, 100.0, 0.0).to(dev)
     S = sum(W * H * K for (W, H, _) in views)
-    # autotune the descent's warp tile on the largest view (the one launch
-    # over all views uses one tile shape); the uneven-batch workload sweeps
-    # tile x leaf size (a leaf size above K changes the sampled indices: each
-    # round stops at the first node holding at most that many splats)
+    # autotune the descent (tile shape, how child masses are shared out, and
+    # for the uneven batch the leaf size: a leaf size above K changes the
+    # sampled indices, each round stopping at the first node holding at most
+    # that many splats) on the whole batch: one sample_views call per
+    # configuration
     from unbiased_differentiable_splatting_gb300 import autotune
     from unbiased_differentiable_splatting_gb300.extensions import transformForward, world2Camera
     from unbiased_differentiable_splatting_gb300.cudaExtensions import transform
-    big = max(range(nviews), key=lambda b: views[b][0] * views[b][1])
     with torch.no_grad():
-        v = slice(big, big + 1)
-        M = transformForward(world2Camera(d["cam_positions"][v], d["cam_orientations"][v]), "-z").squeeze(1)
-        cp = transform.affineForward(M.contiguous(), d["points"])
-        cn = transform.linearForward(M.contiguous(), d["normals"])
+        M = transformForward(world2Camera(d["cam_positions"], d["cam_orientations"]), "-z").squeeze(1).contiguous()
+        cp = transform.affineForward(M, d["points"])
+        cn = transform.linearForward(M, d["normals"])
         cnb = torch.where(cn[..., 2:] > 0, -cn, cn).contiguous()
-        W, H, f = views[big]
-        if wl.get("tune_leaf"):
-            (tile, leaf), tuned = autotune.tune_descent(W, H, f, cp, cnb, d["stddevs"], K, 0.0, wl["precision"],
-                                                        leaf_sizes=autotune.LEAF_CANDIDATES)
-        else:
-            tile, tuned = autotune.tune_descent(W, H, f, cp, cnb, d["stddevs"], K, 0.0, wl["precision"])
-            leaf = 0
-    r.sample_kwargs = {"seed": seed_t, "tile_x": tile, "leaf_size": leaf}
+        best, tuned = autotune.tune_views(views, cp, cnb, d["stddevs"], K, 0.0, wl["precision"],
+                                          leaf_sizes=autotune.LEAF_CANDIDATES if wl.get("tune_leaf") else None)
+        del cp, cn, cnb
+    tile, leaf, spread = best["tile_x"], best.get("leaf_size", 0), best["spread"]
+    r.sample_kwargs = {"seed": seed_t, "tile_x": tile, "leaf_size": leaf, "spread": spread}
 
     def render(pos, quat, pts, nrm, sd, col):
         imgs, _, _ = r(pos, quat, pts, nrm, sd, col, d["ambient"], d["lamp_directions"], d["lamp_intensities"])
@@ -380,6 +376,7 @@ def multiview_main(args, name, wl):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": name, "views": [f"{nv}x{W}x{H}" for (W, H, _, nv) in wl["groups"]],
                    "descent_tile": tile, "leaf_size": leaf if leaf > K else "single-splat leaves (reference rule)",
+                   "child_masses": "spread over the warp" if spread else "per lane",
                    "autotune_ms": {str(k): round(v, 4) for k, v in tuned.items()}, "descent_launches_per_step": 1,
                    "samples_per_step": S, "surfels": wl["n"], "K": K, "shading": wl["shading"],
                    "l2": "flushed (256 MiB write) before each step", "cuda_graph": True},
@@ -640,7 +637,9 @@ def descent_main(args):
         tree = sampling.build_tree(W, H, sc["focal"], cp, cnb, d["stddevs"], K, 0.0, wl["precision"])
     prm, ws = tree["_prm"], tree["_ws"]
     prm.seed = 1234
-    prm.tile_x = autotune.lookup(torch.cuda.get_device_name(dev), W, H, cp.shape[1], K) or 8
+    tuned = autotune.lookup_config(torch.cuda.get_device_name(dev), W, H, cp.shape[1], K) or {}
+    prm.tile_x = tuned.get("tile_x", 8)
+    prm.spread = tuned.get("spread", 0)
     idx = torch.full((W, H, K), -1, dtype=torch.int32, device=dev)
     stream = torch.cuda.current_stream(dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
@@ -662,7 +661,7 @@ def descent_main(args):
         e1.synchronize()
         ts.append(e0.elapsed_time(e1))
     print(json.dumps({"metric": "descent kernel ms", "workload": workload_name("harmonic500k", wl),
-                      "tile_x": prm.tile_x, "steps": args.steps, "warmup": args.warmup,
+                      "tile_x": prm.tile_x, "spread": prm.spread, "steps": args.steps, "warmup": args.warmup,
                       "ms_median": float(np.median(ts)), "visible_splats": tree["n_visible"],
                       "coefficients": tree["n_coefs"]}), flush=True)
 
@@ -779,7 +778,8 @@ def main():
         cp = transform.affineForward(M, d["points"])
         cn = transform.linearForward(M, d["normals"])
         cnb = torch.where(cn[..., 2:] > 0, -cn, cn).contiguous()
-        tile, tile_ms = autotune.tune_descent(W, H, scene["focal"], cp, cnb, d["stddevs"], K, 0.0, wl["precision"])
+        best, tile_ms = autotune.tune_descent(W, H, scene["focal"], cp, cnb, d["stddevs"], K, 0.0, wl["precision"])
+        tile = best["tile_x"]
 
     stream = torch.cuda.current_stream(dev)
     for _ in range(args.warmup):
@@ -864,6 +864,7 @@ def main():
         prm = tree["_prm"]
         prm.seed = 1234
         prm.tile_x = tile
+        prm.spread = best["spread"]
         ws = tree["_ws"]
         idx = torch.full((W, H, K), -1, dtype=torch.int32, device=dev)
         for _ in range(2):
@@ -924,7 +925,9 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": workload_name(args.workload, wl), "l2": L2_NOTE},
             "run": {"parallelism": f"replicas x{world}", "cuda_graph": graph is not None,
-                    "descent_tile": f"{tile}x{32 // tile} pixels per warp (autotuned: "
+                    "descent_tile": f"{tile}x{32 // tile} pixels per warp, child masses "
+                                    + ("spread over the warp" if best["spread"] else "per lane")
+                                    + " (autotuned, tile/spread: "
                                     + ", ".join(f"{k}: {v:.3f} ms" for k, v in sorted(tile_ms.items())) + ")"},
             "e2e": {"value": e2e, "unit": "Msamples/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": 4,
                     "path": ("pinned H2D into the captured step's inputs + CUDA-graph replay of Splatting fwd+bwd "

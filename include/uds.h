@@ -89,6 +89,11 @@ typedef struct {
                                 node holding <= L splats and order-samples
                                 over all of them with their exact Gaussians.
                                 A uniforms tensor is then (B,W,H,R,max(K,L)) */
+    int32_t spread;          /* Poisson descent with K <= 8: how the child
+                                masses below the expansion frontier are shared
+                                out: 0 every lane evaluates its own, 1 spread
+                                over the warp's lanes.  Results are identical;
+                                only the speed differs (the autotuner picks) */
 } uds_sample_params;
 
 /* ---- transform (transform.cpp:33-86: affineForward/Backward,

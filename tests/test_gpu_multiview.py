@@ -54,6 +54,25 @@ def test_sample_views_matches_oracle(smp, K):
                                      T(nrm), T(sd), K, 0.0, 0.01, 77, None)
     for a, b in zip(res, out):
         assert torch.equal(a, b)
+    # every tile shape and both ways of sharing out the child masses agree
+    for tx, sp in ((4, 1), (16, 0), (32, 1)):
+        alt = smp.sample_views(views, T(pts), T(nrm), None, T(sd), K, 0.0, 0.01, seed=77, tile_x=tx, spread=sp)
+        for a, b in zip(alt, out):
+            assert torch.equal(a, b), (tx, sp)
+
+
+def test_tune_views_caches_batch_choice(smp, tmp_path, monkeypatch):
+    from unbiased_differentiable_splatting_gb300 import autotune
+    monkeypatch.setenv("UDS_AUTOTUNE_CACHE", str(tmp_path / "cache.json"))
+    autotune.reset()
+    rng = np.random.default_rng(9)
+    views = [(48, 40, 40.0), (32, 32, 30.0)]
+    pts, nrm, sd = _views_scene(rng, 1500, views)
+    T = lambda a: torch.as_tensor(a).to(DEV)  # noqa: E731
+    best, times = autotune.tune_views(views, T(pts), T(nrm), T(sd), 8, 0.0, 0.01, reps=1, candidates=(8, 16))
+    assert len(times) == 2 * len(autotune.SPREADS)
+    assert autotune.lookup_views(torch.cuda.get_device_name(0), views, pts.shape[1], 8) == best
+    autotune.reset()
 
 
 def test_multiview_renderer(smp):

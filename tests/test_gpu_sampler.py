@@ -246,8 +246,8 @@ def test_stochastic_bit_exact(smp, K):
 
 
 def test_descent_tile_shapes_agree_and_autotune(smp, tmp_path, monkeypatch):
-    """Every warp-tile shape of the descent gives the same indices; the
-    autotuner times them and caches one."""
+    """Every warp-tile shape and both ways of sharing out the child masses
+    give the same indices; the autotuner times them and caches one."""
     from unbiased_differentiable_splatting_gb300 import autotune
     monkeypatch.setenv("UDS_AUTOTUNE_CACHE", str(tmp_path / "cache.json"))
     autotune.reset()
@@ -255,12 +255,14 @@ def test_descent_tile_shapes_agree_and_autotune(smp, tmp_path, monkeypatch):
     W, H, f, N, K = 72, 56, 60.0, 3000, 8
     pts, nrm, sd = camera_scene(rng, N, W, H, f)
     args = (W, H, f, T(pts[None]), T(nrm[None]), T(np.zeros((1, N, 3))), T(sd[None]), K, 0.0, 0.01)
-    ref = smp.sample(*args, seed=3, tile_x=8)
-    for tx in (4, 16, 32):
-        assert torch.equal(smp.sample(*args, seed=3, tile_x=tx), ref), tx
+    ref = smp.sample(*args, seed=3, tile_x=8, spread=0)
+    for tx in (4, 8, 16, 32):
+        for sp in (0, 1):
+            assert torch.equal(smp.sample(*args, seed=3, tile_x=tx, spread=sp), ref), (tx, sp)
     best, times = autotune.tune_descent(W, H, f, T(pts[None]), T(nrm[None]), T(sd[None]), K, 0.0, 0.01)
-    assert best in autotune.CANDIDATES and set(times) == set(autotune.CANDIDATES)
-    assert autotune.lookup(torch.cuda.get_device_name(0), W, H, N, K) == best
+    assert best["tile_x"] in autotune.CANDIDATES and best["spread"] in autotune.SPREADS
+    assert len(times) == len(autotune.CANDIDATES) * len(autotune.SPREADS)
+    assert autotune.lookup_config(torch.cuda.get_device_name(0), W, H, N, K) == best
     assert torch.equal(smp.sample(*args, seed=3), ref)  # now with the tuned tile
     autotune.reset()
 

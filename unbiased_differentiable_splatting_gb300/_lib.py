@@ -28,7 +28,8 @@ class SampleParams(ctypes.Structure):
                 ("K", ctypes.c_int32), ("focal", c_float), ("smoothing", c_float), ("precision", c_float),
                 ("max_degree", ctypes.c_int32), ("std_batch", ctypes.c_int32), ("coef_pool", c_int64),
                 ("seed", c_uint64), ("seed_dev", c_void_p), ("tile_x", ctypes.c_int32),
-                ("fixed_degree", ctypes.c_int32), ("leaf_size", ctypes.c_int32)]
+                ("fixed_degree", ctypes.c_int32), ("leaf_size", ctypes.c_int32),
+                ("spread", ctypes.c_int32)]
 
 
 class ViewDesc(ctypes.Structure):

@@ -1,30 +1,47 @@
 """Autotuner for the per-pixel tree descent (the sampler's dominant kernel).
 
-The descent runs one warp per 32-pixel tile; the tile's width along y
-(``tile_x`` in ``uds_sample_params``: 4, 8, 16 or 32 pixels, the height is
-32 / tile_x) sets how much of the tree the 32 walks of a warp share, and so
-the speed, but not the result: every lane walks its own pixel's tree, so the
-sampled indices are identical for every tile shape.
+Two choices change the descent's speed but not its result:
 
-``tune_descent`` times the descent of one built view for each candidate with
-CUDA events and stores the fastest in a JSON cache keyed by (GPU name, W, H,
-N, K); ``lookup`` is what ``cudaExtensions.sampling.sample`` consults when no
-``tile_x`` is given.  The cache file is ``$UDS_AUTOTUNE_CACHE`` or
+* the warp tile: the descent runs one warp per 32-pixel tile, whose width
+  along y (``tile_x`` in ``uds_sample_params``: 4, 8, 16 or 32 pixels, the
+  height is 32 / tile_x) sets how much of the tree the 32 walks of a warp
+  share; every lane walks its own pixel's tree, so the sampled indices are
+  identical for every tile shape;
+* how the child masses below the expansion frontier are shared out among the
+  lanes (``spread``: 0 every lane evaluates its own, 1 spread over the warp);
+  the masses are the same calls either way.  Spreading is faster where few
+  lanes need masses at a time, evaluating per lane where neighbouring pixels
+  descend the same nodes.
+
+``tune_descent`` times the descent of one built view for each (tile_x,
+spread) pair with CUDA events and stores the fastest in a JSON cache keyed by
+(GPU name, W, H, N, K); ``lookup_config`` is what
+``cudaExtensions.sampling.sample`` consults when no ``tile_x`` / ``spread``
+is given.  The cache file is ``$UDS_AUTOTUNE_CACHE`` or
 ``~/.cache/uds_gb300/autotune.json``.
 
-With ``leaf_sizes`` the sweep covers tile x leaf size.  The leaf size does
+``tune_views`` does the same for a batch of views of different sizes
+(``sampling.sample_views``: every view's tree and one descent launch over
+all of them), timing the whole call for each configuration, because the best
+choice for a batch of small dense views differs from that for its largest
+view; its entry is keyed by the list of view sizes.
+
+With ``leaf_sizes`` the sweep also covers the leaf size.  The leaf size does
 change the sampled indices (``uds_sample_params.leaf_size``: a round stops at
 the first node holding at most max(K, L) splats), so its choice is kept in a
 separate cache entry that only ``sampling.sample(leaf_size="auto")`` reads
-(``lookup_leaf``); the default sampling keeps the reference's rule.
+(``lookup_config(..., leaf=True)``); the default sampling keeps the
+reference's rule.
 """
 from __future__ import annotations
 
+import itertools
 import json
 import os
 import threading
 
 CANDIDATES = (4, 8, 16, 32)
+SPREADS = (0, 1)
 LEAF_CANDIDATES = (0, 16, 32)
 DEFAULT_TILE = 8
 
@@ -39,6 +56,11 @@ def cache_path() -> str:
 
 def key(device_name: str, W: int, H: int, N: int, K: int) -> str:
     return f"{device_name}|descent|W={int(W)}|H={int(H)}|N={int(N)}|K={int(K)}"
+
+
+def views_key(device_name: str, views, N: int, K: int) -> str:
+    sizes = ",".join(f"{int(w)}x{int(h)}" for (w, h, _) in views)
+    return f"{device_name}|views|{sizes}|N={int(N)}|K={int(K)}"
 
 
 def _load() -> dict:
@@ -59,31 +81,51 @@ def reset() -> None:
         _cache = None
 
 
+def _entry(k: str, leaf: bool):
+    with _lock:
+        e = _load().get(k + ("|leaf" if leaf else ""))
+    if not e:
+        return None
+    out = {"tile_x": int(e["tile_x"]), "spread": int(e.get("spread", 0))}
+    if leaf:
+        out["leaf_size"] = int(e["leaf_size"])
+    return out
+
+
+def lookup_config(device_name: str, W: int, H: int, N: int, K: int, leaf: bool = False):
+    """Cached descent configuration for this shape, {"tile_x", "spread"}
+    (plus "leaf_size" for the sweep with leaf sizes, ``leaf=True``), or
+    None."""
+    return _entry(key(device_name, W, H, N, K), leaf)
+
+
+def lookup_views(device_name: str, views, N: int, K: int, leaf: bool = False):
+    """Cached configuration of ``tune_views`` for this list of view sizes, or
+    None."""
+    return _entry(views_key(device_name, views, N, K), leaf)
+
+
 def lookup(device_name: str, W: int, H: int, N: int, K: int):
     """Cached tile width for this shape, or None."""
-    with _lock:
-        e = _load().get(key(device_name, W, H, N, K))
-    return int(e["tile_x"]) if e else None
+    e = lookup_config(device_name, W, H, N, K)
+    return e["tile_x"] if e else None
 
 
 def lookup_leaf(device_name: str, W: int, H: int, N: int, K: int):
-    """Cached (tile_x, leaf_size) of a tile x leaf sweep for this shape, or
-    None."""
-    with _lock:
-        e = _load().get(key(device_name, W, H, N, K) + "|leaf")
-    return (int(e["tile_x"]), int(e["leaf_size"])) if e else None
+    """Cached (tile_x, leaf_size) of a sweep with leaf sizes, or None."""
+    e = lookup_config(device_name, W, H, N, K, leaf=True)
+    return (e["tile_x"], e["leaf_size"]) if e else None
 
 
-def record(device_name: str, W: int, H: int, N: int, K: int, tile_x: int, timings_ms: dict,
-           leaf_size=None) -> None:
+def record(device_name: str, W: int, H: int, N: int, K: int, config: dict, timings_ms: dict, views=None) -> None:
+    """Store `config` ({"tile_x", "spread"[, "leaf_size"]}) for this shape
+    (or for this list of views)."""
     with _lock:
         c = _load()
-        entry = {"tile_x": int(tile_x), "ms": {str(k): float(v) for k, v in timings_ms.items()}}
-        k = key(device_name, W, H, N, K)
-        if leaf_size is not None:
-            entry["leaf_size"] = int(leaf_size)
-            k += "|leaf"
-        c[k] = entry
+        entry = {k: int(v) for k, v in config.items()}
+        entry["ms"] = {str(k): float(v) for k, v in timings_ms.items()}
+        k = key(device_name, W, H, N, K) if views is None else views_key(device_name, views, N, K)
+        c[k + ("|leaf" if "leaf_size" in config else "")] = entry
         path = cache_path()
         os.makedirs(os.path.dirname(path), exist_ok=True)
         tmp = path + f".tmp{os.getpid()}"
@@ -92,20 +134,19 @@ def record(device_name: str, W: int, H: int, N: int, K: int, tile_x: int, timing
         os.replace(tmp, path)
 
 
-def choose(timings_ms: dict) -> int:
-    """Fastest candidate (ties: the smaller tile)."""
+def choose(timings_ms: dict):
+    """Fastest candidate (ties: the first in sorted order, i.e. the smaller
+    tile)."""
     return min(sorted(timings_ms), key=lambda t: timings_ms[t])
 
 
 def tune_descent(width, height, focallength, points, normals, stdDevs, numSamples, smoothing, precision,
-                 view=0, reps=3, candidates=CANDIDATES, timer=None, save=True, leaf_sizes=None):
-    """Time the descent of view `view` for each candidate tile width and cache
-    the fastest.  `timer(tile_x) -> ms` replaces the GPU timing (tests).
-    Returns (best tile_x, {tile_x: ms}).
-
-    With `leaf_sizes` (e.g. LEAF_CANDIDATES) every (tile_x, leaf_size) pair is
-    timed, `timer(tile_x, leaf_size)`, and the fastest pair is cached for
-    ``lookup_leaf``; returns ((tile_x, leaf_size), {"tile/leaf": ms})."""
+                 view=0, reps=3, candidates=CANDIDATES, timer=None, save=True, leaf_sizes=None, spreads=SPREADS):
+    """Time the descent of view `view` for each (tile_x, spread) pair, and
+    each leaf size of `leaf_sizes` when given (e.g. LEAF_CANDIDATES), and
+    cache the fastest.  `timer(tile_x, spread, leaf_size) -> ms` replaces the
+    GPU timing (tests).  Returns (best configuration {"tile_x", "spread"
+    [, "leaf_size"]}, {"tile/spread[/leaf]": ms})."""
     import torch
     from ._lib import check, load, stream_ptr
     from .cudaExtensions import sampling
@@ -120,8 +161,9 @@ def tune_descent(width, height, focallength, points, normals, stdDevs, numSample
         idx = torch.empty((W, H, K), dtype=torch.int32, device=dev)
         stream = torch.cuda.current_stream(dev)
 
-        def timer(tx, leaf=0):
+        def timer(tx, spread, leaf):
             prm.tile_x = tx
+            prm.spread = spread
             prm.leaf_size = leaf
             ts = []
             for r in range(reps + 1):
@@ -135,15 +177,55 @@ def tune_descent(width, height, focallength, points, normals, stdDevs, numSample
                 if r:
                     ts.append(e0.elapsed_time(e1))
             return min(ts)
-    if leaf_sizes is not None:
-        pairs = {(int(t), int(lf)): float(timer(int(t), int(lf))) for t in candidates for lf in leaf_sizes}
-        tb, lb = min(sorted(pairs), key=lambda q: pairs[q])
-        timings = {f"{t}/{lf}": v for (t, lf), v in pairs.items()}
-        if save:
-            record(name, W, H, N, K, tb, timings, leaf_size=lb)
-        return (tb, lb), timings
-    timings = {int(t): float(timer(int(t))) for t in candidates}
-    best = choose(timings)
+    best, timings = _sweep(timer, candidates, spreads, leaf_sizes)
     if save:
         record(name, W, H, N, K, best, timings)
+    return best, timings
+
+
+def _sweep(timer, candidates, spreads, leaf_sizes):
+    leaves = tuple(leaf_sizes) if leaf_sizes is not None else (0,)
+    pairs = {(int(t), int(s), int(lf)): float(timer(int(t), int(s), int(lf)))
+             for t, s, lf in itertools.product(candidates, spreads, leaves)}
+    t, s, lf = choose(pairs)
+    best = {"tile_x": t, "spread": s}
+    if leaf_sizes is not None:
+        best["leaf_size"] = lf
+        timings = {f"{a}/{b}/{c}": v for (a, b, c), v in pairs.items()}
+    else:
+        timings = {f"{a}/{b}": v for (a, b, _), v in pairs.items()}
+    return best, timings
+
+
+def tune_views(views, points, normals, stdDevs, numSamples, smoothing, precision, reps=3, candidates=CANDIDATES,
+               timer=None, save=True, leaf_sizes=None, spreads=SPREADS):
+    """``tune_descent`` for a batch of views of different sizes (``views``: B
+    (width, height, focallength); points / normals (B,N,3) in camera space):
+    every configuration times a whole ``sampling.sample_views`` call.  The
+    result is cached for this list of view sizes, which ``sample_views``
+    consults."""
+    import torch
+    from .cudaExtensions import sampling
+    dev = points.device
+    name = torch.cuda.get_device_name(dev) if timer is None else "test-device"
+    N, K = int(points.shape[1]), int(numSamples)
+    if timer is None:
+        stream = torch.cuda.current_stream(dev)
+
+        def timer(tx, spread, leaf):
+            ts = []
+            for r in range(reps + 1):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                sampling.sample_views(views, points, normals, None, stdDevs, K, smoothing, precision, seed=1,
+                                      tile_x=tx, leaf_size=leaf, spread=spread)
+                e1.record(stream)
+                e1.synchronize()
+                if r:
+                    ts.append(e0.elapsed_time(e1))
+            return min(ts)
+    best, timings = _sweep(timer, candidates, spreads, leaf_sizes)
+    if save:
+        record(name, 0, 0, N, K, best, timings, views=views)
     return best, timings

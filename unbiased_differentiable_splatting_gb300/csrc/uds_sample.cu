@@ -583,14 +583,18 @@ __global__ void k_assign(ViewState* vs, float4* cen, const uint32_t* __restrict_
 // ----------------------------------------------------------------- 7 P2M
 // shiftLeafHermiteExpansion (hermitefmm.cuh:119-138) summed per node over
 // its leaves in Morton order: C_ab = sum_i t_a(s0_i) t_b(s1_i) with
-// t_a(s) = s^a / a!, s = (leaf - centre) * (1 / sqrt(2 h^2)).  One warp per
-// internal node.  For a chunk of 32 leaves each lane builds one leaf's
+// t_a(s) = s^a / a!, s = (leaf - centre) * (1 / sqrt(2 h^2)).  A warp builds
+// one node at a time.  For a chunk of 32 leaves each lane builds one leaf's
 // t-tables in shared memory (t_a = (t_{a-1} s) * (1 / a)); each lane then
 // owns a block of BR rows x BC columns of C (the block shape depends on the
 // degree, so that the blocks of a (p+1)^2 table fit 32 lanes) and adds
 // fma(t_a(s0), t_b(s1), C_ab) leaf by leaf: every coefficient is summed in
 // leaf order exactly as the oracle's deterministic flavour does, and one
-// shared-memory read feeds BR or BC multiply-adds.
+// shared-memory read feeds BR or BC multiply-adds.  A warp takes 32
+// consecutive nodes (one coalesced read of their records and links) and
+// builds their expansions one after another: one node per warp left the
+// kernel waiting on two dependent memory round trips per few hundred
+// multiply-adds.
 constexpr int kP2MWarps = 4;
 // 1 / a, rounded once at compile time (the oracle uses the same constants)
 __constant__ float kInvInt[kMaxDegree + 1] = {0.0f, 1.0f / 1, 1.0f / 2, 1.0f / 3, 1.0f / 4, 1.0f / 5, 1.0f / 6,
@@ -624,73 +628,89 @@ __global__ void __launch_bounds__(32 * kP2MWarps) k_p2m(const ViewState* vs, con
                                                         float* __restrict__ coef) {
     __shared__ float s_tx[kP2MWarps][32 * kTStride];
     __shared__ float s_ty[kP2MWarps][32 * kTStride];
+    const unsigned full = 0xffffffffu;
     int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    int v = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    if (v >= vs->n - 1) return;  // uniform over the warp
-    float4 c = cen[v];
-    int p = meta_degree(c.w);
-    if (p < 0) return;
-    int off = meta_offset(c.w);
-    int4 L = lnk[v];
+    int n = vs->n;
     float isq = vs->isq;
-    int P1 = p + 1;
-    int BR = kP2MBlock[P1][0], BC = kP2MBlock[P1][1];
-    int nC = (P1 + BC - 1) / BC, nR = (P1 + BR - 1) / BR;
-    int gr = lane / nC, gc = lane % nC;
-    bool owner = gr < nR;
-    // this lane's rows and columns; reads past the table repeat its last
-    // row / column (their sums are not written)
-    int ra[3], cb[4];
-#pragma unroll
-    for (int i = 0; i < 3; ++i) ra[i] = min(gr * BR + i, p);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) cb[k] = min(gc * BC + k, p);
-    float acc[3][4];
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int k = 0; k < 4; ++k) acc[i][k] = 0.0f;
+    // 32 consecutive internal nodes per warp: lane l loads node v0 + l's
+    // record and links (one coalesced read), then the warp builds the nodes'
+    // expansions one after another
+    int v0 = (int)((((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32);
+    if (v0 >= n - 1) return;  // uniform over the warp
+    int vl = v0 + lane;
+    bool inner = vl < n - 1;
+    float4 cl = inner ? cen[vl] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    int4 Ll = inner ? lnk[vl] : make_int4(0, 0, 0, 0);
+    unsigned todo = __ballot_sync(full, inner && meta_degree(cl.w) >= 0);
     float* tx = s_tx[warp];
     float* ty = s_ty[warp];
-    int end = L.z + L.w;
-    for (int i0 = L.z; i0 < end; i0 += 32) {
-        int cnt = min(32, end - i0);
-        if (lane < cnt) {
-            float2 q = leaf_xy[i0 + lane];
-            float s0 = fmul(fsub(q.x, c.x), isq);
-            float s1 = fmul(fsub(q.y, c.y), isq);
-            float ax = 1.0f, ay = 1.0f;
-            tx[lane * kTStride] = 1.0f;
-            ty[lane * kTStride] = 1.0f;
-            for (int a = 1; a <= p; ++a) {
-                ax = fmul(fmul(ax, s0), kInvInt[a]);
-                ay = fmul(fmul(ay, s1), kInvInt[a]);
-                tx[lane * kTStride + a] = ax;
-                ty[lane * kTStride + a] = ay;
-            }
-        }
-        __syncwarp();
-        if (owner) {
-            switch (BR * 8 + BC) {  // uniform over the warp
-                case 9: p2m_block<1, 1>(tx, ty, cnt, ra, cb, acc); break;
-                case 10: p2m_block<1, 2>(tx, ty, cnt, ra, cb, acc); break;
-                case 11: p2m_block<1, 3>(tx, ty, cnt, ra, cb, acc); break;
-                case 18: p2m_block<2, 2>(tx, ty, cnt, ra, cb, acc); break;
-                case 19: p2m_block<2, 3>(tx, ty, cnt, ra, cb, acc); break;
-                case 20: p2m_block<2, 4>(tx, ty, cnt, ra, cb, acc); break;
-                default: p2m_block<3, 4>(tx, ty, cnt, ra, cb, acc); break;
-            }
-        }
-        __syncwarp();
-    }
-    if (owner) {
+    while (todo) {
+        int k = __ffs(todo) - 1;
+        todo &= todo - 1;
+        float4 c;
+        c.x = __shfl_sync(full, cl.x, k);
+        c.y = __shfl_sync(full, cl.y, k);
+        c.w = __shfl_sync(full, cl.w, k);
+        int first = __shfl_sync(full, Ll.z, k), count = __shfl_sync(full, Ll.w, k);
+        int p = meta_degree(c.w);
+        int off = meta_offset(c.w);
+        int P1 = p + 1;
+        int BR = kP2MBlock[P1][0], BC = kP2MBlock[P1][1];
+        int nC = (P1 + BC - 1) / BC, nR = (P1 + BR - 1) / BR;
+        int gr = lane / nC, gc = lane % nC;
+        bool owner = gr < nR;
+        // this lane's rows and columns; reads past the table repeat its last
+        // row / column (their sums are not written)
+        int ra[3], cb[4];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) ra[i] = min(gr * BR + i, p);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) cb[q] = min(gc * BC + q, p);
+        float acc[3][4];
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                int a = gr * BR + i, b = gc * BC + k;
-                if (i < BR && k < BC && a <= p && b <= p) coef[off + a * P1 + b] = acc[i][k];
+            for (int q = 0; q < 4; ++q) acc[i][q] = 0.0f;
+        int end = first + count;
+        for (int i0 = first; i0 < end; i0 += 32) {
+            int cnt = min(32, end - i0);
+            if (lane < cnt) {
+                float2 q = leaf_xy[i0 + lane];
+                float s0 = fmul(fsub(q.x, c.x), isq);
+                float s1 = fmul(fsub(q.y, c.y), isq);
+                float ax = 1.0f, ay = 1.0f;
+                tx[lane * kTStride] = 1.0f;
+                ty[lane * kTStride] = 1.0f;
+                for (int a = 1; a <= p; ++a) {
+                    ax = fmul(fmul(ax, s0), kInvInt[a]);
+                    ay = fmul(fmul(ay, s1), kInvInt[a]);
+                    tx[lane * kTStride + a] = ax;
+                    ty[lane * kTStride + a] = ay;
+                }
             }
+            __syncwarp();
+            if (owner) {
+                switch (BR * 8 + BC) {  // uniform over the warp
+                    case 9: p2m_block<1, 1>(tx, ty, cnt, ra, cb, acc); break;
+                    case 10: p2m_block<1, 2>(tx, ty, cnt, ra, cb, acc); break;
+                    case 11: p2m_block<1, 3>(tx, ty, cnt, ra, cb, acc); break;
+                    case 18: p2m_block<2, 2>(tx, ty, cnt, ra, cb, acc); break;
+                    case 19: p2m_block<2, 3>(tx, ty, cnt, ra, cb, acc); break;
+                    case 20: p2m_block<2, 4>(tx, ty, cnt, ra, cb, acc); break;
+                    default: p2m_block<3, 4>(tx, ty, cnt, ra, cb, acc); break;
+                }
+            }
+            __syncwarp();
+        }
+        if (owner) {
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    int a = gr * BR + i, b = gc * BC + q;
+                    if (i < BR && q < BC && a <= p && b <= p) coef[off + a * P1 + b] = acc[i][q];
+                }
+        }
     }
 }
 
@@ -1011,36 +1031,52 @@ __device__ void warp_root_walk(const Tree& T, float qx, float qy, bool live, Mas
 }
 
 // Child masses (w0, w1) = getWeight of the children (a, b) for every lane
-// of the warp with `need` (all lanes call this together).  The 2c
-// evaluations of the c lanes that need them are spread over the warp's 32
-// lanes, evaluation e being the child e % 2 of the (e / 2)-th needing lane
-// (in lane order), so a lane waits for one series instead of two while c <=
-// 16; the value of each is the same node_weight call whichever lane makes
-// it.  `owner`: 32 ints of the warp's shared memory.
+// of the warp with `need` (all lanes call this together); the value of each
+// is the same node_weight call whichever lane makes it, so both forms below
+// give identical masses, only the speed differs (the autotuner picks one per
+// view shape; uds_sample_params.spread).
+// SPREAD false: every needing lane evaluates its own two children, left then
+//   right; neighbouring pixels at the same node evaluate the same child side
+//   by side (equal trip counts, one coefficient stream).
+// SPREAD true: the 2c evaluations of the c needing lanes are spread over the
+//   warp's 32 lanes, first the left children of the needing lanes (in lane
+//   order), then their right children, so a lane waits for one series
+//   instead of two while c <= 16.  `owner`: 32 ints of the warp's shared
+//   memory.
+template <bool SPREAD>
 __device__ __forceinline__ void warp_child_masses(const Tree& T, bool need, int a, int b, float qx, float qy,
                                                   float& w0, float& w1, int* owner) {
+    if (!SPREAD) {
+        if (need) {
+#pragma unroll 1
+            for (int ch = 0; ch < 2; ++ch) {
+                float x = fmaxf(0.0f, node_weight(T, ch ? b : a, qx, qy));
+                if (ch) w1 = x; else w0 = x;
+            }
+        }
+        return;
+    }
     const unsigned full = 0xffffffffu;
     unsigned nm = __ballot_sync(full, need);
     if (!nm) return;
     const int lane = (threadIdx.x + blockDim.x * threadIdx.y) & 31;
-    int c2 = 2 * __popc(nm);
+    int c = __popc(nm), c2 = 2 * c;
     int rank = __popc(nm & ((1u << lane) - 1u));
     if (need) owner[rank] = lane;
     __syncwarp();
 #pragma unroll 1
     for (int e0 = 0; e0 < c2; e0 += 32) {
         int e = e0 + lane;
-        int o = e < c2 ? owner[e >> 1] : lane;
+        bool right = e >= c;
+        int o = e < c2 ? owner[right ? e - c : e] : lane;
         float oqx = __shfl_sync(full, qx, o), oqy = __shfl_sync(full, qy, o);
         int oa = __shfl_sync(full, a, o), ob = __shfl_sync(full, b, o);
         float x = 0.0f;
-        if (e < c2) x = fmaxf(0.0f, node_weight(T, (e & 1) ? ob : oa, oqx, oqy));
-        int src = 2 * rank - e0;  // the lane holding this lane's first child in this pass
-        float x0 = __shfl_sync(full, x, src & 31), x1 = __shfl_sync(full, x, (src + 1) & 31);
-        if (need && src >= 0 && src < 32) {
-            w0 = x0;
-            w1 = x1;
-        }
+        if (e < c2) x = fmaxf(0.0f, node_weight(T, right ? ob : oa, oqx, oqy));
+        int s0 = rank - e0, s1 = c + rank - e0;  // lanes holding this lane's children in this pass
+        float x0 = __shfl_sync(full, x, s0 & 31), x1 = __shfl_sync(full, x, s1 & 31);
+        if (need && s0 >= 0 && s0 < 32) w0 = x0;
+        if (need && s1 >= 0 && s1 < 32) w1 = x1;
     }
     __syncwarp();  // owner is rewritten by the next call
 }
@@ -1057,7 +1093,7 @@ struct UnevenViews {
     long long ioff[kMaxUneven];
 };
 
-template <int R, int KM, bool UNEVEN>
+template <int R, int KM, bool UNEVEN, bool SPREAD>
 __global__ void __launch_bounds__(128, 4) k_sample(Tree T, const ViewState* vs, int W, int H, int K,
                                                 int M, float precision, const float* __restrict__ uniforms,
                                                 uint64_t seed, const uint64_t* __restrict__ seed_ptr,
@@ -1169,7 +1205,7 @@ __global__ void __launch_bounds__(128, 4) k_sample(Tree T, const ViewState* vs, 
             // a child is one expansion, so the divergence is only in the
             // series' trip counts); one call site keeps the walk inlined once,
             // small enough for the instruction cache
-            warp_child_masses(T, need, a, b, qx, qy, w0, w1, ws_owner);
+            warp_child_masses<SPREAD>(T, need, a, b, qx, qy, w0, w1, ws_owner);
             if (going) {
                 // (re)write unconditionally: a hit stores the same masses, and
                 // a store does not wait on the per-thread memory like a load
@@ -1348,7 +1384,7 @@ __global__ void __launch_bounds__(128, 4) k_stochastic(Tree T, const ViewState* 
             }
             // every lane that needs its node's child masses gets them in the
             // same pass (one call site: the walk is inlined once)
-            warp_child_masses(T, need, a, b, qx, qy, w0, w1, s_walk[warp].right);
+            warp_child_masses<false>(T, need, a, b, qx, qy, w0, w1, s_walk[warp].right);
             if (going) {
                 cv[d] = v;
                 cw0[d] = w0;
@@ -1718,7 +1754,7 @@ static int build_view(const uds_sample_params* p, const Ws& w, int view, const f
     k_scan_top<<<1, 1024, 0, s>>>(w.scanTmp, (int)sb);
     k_scan_down<<<sb, kScanThreads, 0, s>>>(w.sizes, w.vs, 1, 0, w.scanTmp, w.offsets);
     k_assign<<<nbN, 128, 0, s>>>(w.vs, w.cen, w.sizes, w.offsets, w.coef_cap, w.stats + view);
-    k_p2m<<<cdiv((size_t)N * 32, 128), 128, 0, s>>>(w.vs, w.lnk, w.cen, w.leaf_xy, w.coef);
+    k_p2m<<<cdiv((size_t)N, 32 * kP2MWarps), 32 * kP2MWarps, 0, s>>>(w.vs, w.lnk, w.cen, w.leaf_xy, w.coef);
     k_finish_view<<<1, 1, 0, s>>>(w.vs, w.stats + view);
     return launch_status(6);
 }
@@ -1749,16 +1785,21 @@ static void launch_sample(const Tree& T, const Ws& w, const uds_sample_params* p
     const int M = candidates(p);
     size_t ustride = (size_t)p->W * p->H * R * M;
     UnevenViews none{};
-    if (R <= 3 && p->K <= 8)
-        k_sample<(R <= 3 ? R : 3), 8, false><<<grid, block, 0, s>>>(T, w.vs, p->W, p->H, p->K, M, p->precision, u,
-                                                                    p->seed, p->seed_dev, (uint32_t)view, idx,
-                                                                    w.stats + view, vstride, ustride, istride, none);
-    else
-        k_sample<(R >= 3 ? R : 3), kMaxK, false><<<grid, block, 0, s>>>(T, w.vs, p->W, p->H, p->K, M, p->precision,
-                                                                        u,
-                                                                        p->seed, p->seed_dev, (uint32_t)view, idx,
-                                                                        w.stats + view, vstride, ustride, istride,
-                                                                        none);
+    if (R <= 3 && p->K <= 8) {
+        constexpr int RR = R <= 3 ? R : 3;
+        if (p->spread)
+            k_sample<RR, 8, false, true><<<grid, block, 0, s>>>(T, w.vs, p->W, p->H, p->K, M, p->precision, u, p->seed,
+                                                                p->seed_dev, (uint32_t)view, idx, w.stats + view,
+                                                                vstride, ustride, istride, none);
+        else
+            k_sample<RR, 8, false, false><<<grid, block, 0, s>>>(T, w.vs, p->W, p->H, p->K, M, p->precision, u,
+                                                                 p->seed, p->seed_dev, (uint32_t)view, idx,
+                                                                 w.stats + view, vstride, ustride, istride, none);
+    } else {
+        k_sample<(R >= 3 ? R : 3), kMaxK, false, false><<<grid, block, 0, s>>>(
+            T, w.vs, p->W, p->H, p->K, M, p->precision, u, p->seed, p->seed_dev, (uint32_t)view, idx,
+            w.stats + view, vstride, ustride, istride, none);
+    }
 }
 
 // Views of different sizes (K <= 8) in one launch: a one-dimensional grid of
@@ -1768,9 +1809,14 @@ static void launch_sample_uneven(const Tree& T, const Ws& w, const uds_sample_pa
                                  int* idx, cudaStream_t s, size_t vstride) {
     int tx = p->tile_x > 0 ? p->tile_x : 8;
     dim3 block(tx, 128 / tx);
-    k_sample<R, 8, true><<<uv.first[uv.nv], block, 0, s>>>(T, w.vs, 0, 0, p->K, candidates(p), p->precision,
-                                                           nullptr, p->seed,
-                                                           p->seed_dev, 0u, idx, w.stats, vstride, 0, 0, uv);
+    if (p->spread)
+        k_sample<R, 8, true, true><<<uv.first[uv.nv], block, 0, s>>>(T, w.vs, 0, 0, p->K, candidates(p), p->precision,
+                                                                     nullptr, p->seed, p->seed_dev, 0u, idx, w.stats,
+                                                                     vstride, 0, 0, uv);
+    else
+        k_sample<R, 8, true, false><<<uv.first[uv.nv], block, 0, s>>>(T, w.vs, 0, 0, p->K, candidates(p),
+                                                                      p->precision, nullptr, p->seed, p->seed_dev,
+                                                                      0u, idx, w.stats, vstride, 0, 0, uv);
 }
 
 static int check_params(const uds_sample_params* p) {
@@ -1783,6 +1829,7 @@ static int check_params(const uds_sample_params* p) {
     if (p->tile_x != 0 && p->tile_x != 4 && p->tile_x != 8 && p->tile_x != 16 && p->tile_x != 32)
         return UDS_ERR_ARGUMENT;
     if (p->leaf_size < 0 || p->leaf_size > kMaxLeaf) return UDS_ERR_ARGUMENT;
+    if (p->spread != 0 && p->spread != 1) return UDS_ERR_ARGUMENT;
     if (p->fixed_degree != 0) {
         if (p->fixed_degree != 4 && p->fixed_degree != 6 && p->fixed_degree != 8) return UDS_ERR_ARGUMENT;
         int64_t need = (int64_t)(p->N > 1 ? p->N - 1 : 0) * (p->fixed_degree + 1) * (p->fixed_degree + 1);

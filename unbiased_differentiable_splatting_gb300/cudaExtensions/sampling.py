@@ -20,6 +20,9 @@ end so existing calls keep working:
 * ``tile_x``: width of the descent's 32-pixel warp tiles (4, 8, 16, 32);
   default: the autotuner's cached choice for this shape (see ``autotune``),
   else 8.  The indices do not depend on it.
+* ``spread``: 0 or 1, how the descent shares out the child masses below the
+  expansion frontier among a warp's lanes (K <= 8); default: the
+  autotuner's cached choice, else 0.  The indices do not depend on it.
 * ``leaf_size``: 0 or <= K (default): the reference's single-splat leaves.
   K < L <= 64 (no reference counterpart): leaf buckets of L splats; each round
   of the descent stops at the first node holding <= L splats and
@@ -54,7 +57,7 @@ def num_rounds(K: int) -> int:
 
 
 def params(width, height, focallength, points, stdDevs, numSamples, smoothing, precision, seed=0,
-           max_degree=MAX_DEGREE, coef_pool=0, tile_x=0, fixed_degree=0, leaf_size=0) -> SampleParams:
+           max_degree=MAX_DEGREE, coef_pool=0, tile_x=0, fixed_degree=0, leaf_size=0, spread=0) -> SampleParams:
     """``seed``: an int, or a one-element int64 CUDA tensor whose value the
     kernels read when they run (a captured CUDA graph then draws new numbers
     after the tensor is updated)."""
@@ -62,7 +65,7 @@ def params(width, height, focallength, points, stdDevs, numSamples, smoothing, p
                        focal=float(focallength), smoothing=float(smoothing), precision=float(precision),
                        max_degree=int(max_degree), std_batch=stdDevs.shape[0], coef_pool=int(coef_pool or 0),
                        seed=0, seed_dev=None, tile_x=int(tile_x or 0), fixed_degree=int(fixed_degree or 0),
-                       leaf_size=int(leaf_size or 0))
+                       leaf_size=int(leaf_size or 0), spread=int(spread or 0))
     if isinstance(seed, torch.Tensor):
         if seed.dtype != torch.int64 or seed.numel() != 1 or seed.device != points.device:
             raise ValueError("a seed tensor must be one int64 element on the points' device")
@@ -90,6 +93,42 @@ def _check(points, normals, stdDevs):
         raise ValueError("stdDevs must be (1|B,N,2)")
 
 
+def _descent(points, width, height, numSamples, tile_x=None, leaf_size=0, spread=None):
+    """(tile_x, leaf_size, spread) of the descent: the given values, else the
+    autotuner's cached choices for this shape (``leaf_size="auto"``: those of
+    its sweep with leaf sizes), else the defaults (8, 0, 0)."""
+    from .. import autotune
+    auto_leaf = leaf_size == "auto"
+    if tile_x and spread is not None and not auto_leaf:
+        return int(tile_x), int(leaf_size or 0), int(spread)
+    name = _device_name(points.device)
+    e = autotune.lookup_config(name, width, height, points.shape[1], numSamples, leaf=auto_leaf)
+    if e is None and auto_leaf:
+        e = autotune.lookup_config(name, width, height, points.shape[1], numSamples)
+    e = e or {}
+    return (int(tile_x) if tile_x else e.get("tile_x", autotune.DEFAULT_TILE),
+            e.get("leaf_size", 0) if auto_leaf else int(leaf_size or 0),
+            int(spread) if spread is not None else e.get("spread", 0))
+
+
+def _descent_views(views, points, numSamples, tile_x=None, leaf_size=0, spread=None):
+    """``_descent`` for a batch of views: the cached choices of
+    ``autotune.tune_views`` for this list of view sizes, else those for the
+    first view's shape."""
+    from .. import autotune
+    auto_leaf = leaf_size == "auto"
+    if not (tile_x and spread is not None and not auto_leaf):
+        e = autotune.lookup_views(_device_name(points.device), views, points.shape[1], numSamples, leaf=auto_leaf)
+        if e is not None:
+            return (int(tile_x) if tile_x else e["tile_x"], e.get("leaf_size", 0) if auto_leaf else int(leaf_size or 0),
+                    int(spread) if spread is not None else e["spread"])
+    W0, H0, _ = views[0]
+    return _descent(points, W0, H0, numSamples, tile_x, leaf_size, spread)
+
+
+_device_names = {}
+
+
 def _device_name(dev):
     name = _device_names.get(dev.index)
     if name is None:
@@ -97,43 +136,18 @@ def _device_name(dev):
     return name
 
 
-def _tile(points, width, height, numSamples, tile_x):
-    """Descent tile width: the given one, else the autotuner's cached choice
-    for this shape, else the default."""
-    if tile_x:
-        return int(tile_x)
-    from .. import autotune
-    t = autotune.lookup(_device_name(points.device), width, height, points.shape[1], numSamples)
-    return t or autotune.DEFAULT_TILE
-
-
-def _leaf(points, width, height, numSamples, tile_x, leaf_size):
-    """(tile_x, leaf_size) with ``leaf_size="auto"`` resolved from the
-    autotuner's tile x leaf sweep."""
-    if leaf_size != "auto":
-        return _tile(points, width, height, numSamples, tile_x), int(leaf_size or 0)
-    from .. import autotune
-    e = autotune.lookup_leaf(_device_name(points.device), width, height, points.shape[1], numSamples)
-    if e is None:
-        return _tile(points, width, height, numSamples, tile_x), 0
-    return (int(tile_x) if tile_x else e[0]), e[1]
-
-
-_device_names = {}
-
-
 def sample(width: int, height: int, focallength: float, points, normals, colors, stdDevs, numSamples: int,
            smoothing: float, precision: float, uniforms=None, seed=None, h=None, return_stats=False,
-           max_degree=MAX_DEGREE, coef_pool=0, tile_x=None, fixed_degree=0, leaf_size=0):
+           max_degree=MAX_DEGREE, coef_pool=0, tile_x=None, fixed_degree=0, leaf_size=0, spread=None):
     _check(points, normals, stdDevs)
     dev = points.device
     B = points.shape[0]
     K = int(numSamples)
     if seed is None:
         seed = int(torch.randint(0, 2 ** 62, (1,)).item())
-    tile_x, leaf_size = _leaf(points, width, height, K, tile_x, leaf_size)
+    tile_x, leaf_size, spread = _descent(points, width, height, K, tile_x, leaf_size, spread)
     prm = params(width, height, focallength, points, stdDevs, K, smoothing, precision, seed, max_degree, coef_pool,
-                 tile_x, fixed_degree, leaf_size)
+                 tile_x, fixed_degree, leaf_size, spread)
     if uniforms is not None:
         need(uniforms, "uniforms", device=dev)
         R, M = num_rounds(K), max(K, int(leaf_size or 0))
@@ -156,7 +170,7 @@ def sample(width: int, height: int, focallength: float, points, normals, colors,
 
 def sample_views(views, points, normals, colors, stdDevs, numSamples: int, smoothing: float, precision: float,
                  seed=None, h=None, return_stats=False, max_degree=MAX_DEGREE, coef_pool=0, tile_x=None,
-                 fixed_degree=0, leaf_size=0):
+                 fixed_degree=0, leaf_size=0, spread=None):
     """sampling.sample for B views of different sizes in one call (no
     reference counterpart): ``views`` is a list of B (width, height,
     focallength); points / normals (B,N,3), stdDevs (1|B,N,2).  Every view's
@@ -172,9 +186,9 @@ def sample_views(views, points, normals, colors, stdDevs, numSamples: int, smoot
     if seed is None:
         seed = int(torch.randint(0, 2 ** 62, (1,)).item())
     W0, H0, f0 = views[0]
-    tile_x, leaf_size = _leaf(points, W0, H0, K, tile_x, leaf_size)
+    tile_x, leaf_size, spread = _descent_views(views, points, K, tile_x, leaf_size, spread)
     prm = params(W0, H0, f0, points, stdDevs, K, smoothing, precision, seed, max_degree, coef_pool, tile_x,
-                 fixed_degree, leaf_size)
+                 fixed_degree, leaf_size, spread)
     desc = (ViewDesc * B)(*[ViewDesc(int(w), int(hh), float(f), 0) for (w, hh, f) in views])
     if h is not None:
         need(h, "h", device=dev)
