@@ -613,8 +613,9 @@ def next_rows_main(args):
 def descent_main(args):
     """The per-pixel descent kernel alone on the harmonic 500k / 1024^2 view
     (the tree built once, then --warmup untimed and --steps timed launches
-    with the tile the autotuner caches, else 8 pixels wide): the small,
-    self-contained command the ncu captures of k_sample run on."""
+    with --tile / --spread when given, else the autotuner's cached choice,
+    else 8 pixels wide and child masses per lane): the small, self-contained
+    command the ncu captures of k_sample run on."""
     import torch
     from unbiased_differentiable_splatting_gb300 import _lib, autotune, load
     from unbiased_differentiable_splatting_gb300.extensions import transformForward, world2Camera
@@ -638,8 +639,8 @@ def descent_main(args):
     prm, ws = tree["_prm"], tree["_ws"]
     prm.seed = 1234
     tuned = autotune.lookup_config(torch.cuda.get_device_name(dev), W, H, cp.shape[1], K) or {}
-    prm.tile_x = tuned.get("tile_x", 8)
-    prm.spread = tuned.get("spread", 0)
+    prm.tile_x = args.tile or tuned.get("tile_x", 8)
+    prm.spread = args.spread if args.spread is not None else tuned.get("spread", 0)
     idx = torch.full((W, H, K), -1, dtype=torch.int32, device=dev)
     stream = torch.cuda.current_stream(dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
@@ -678,6 +679,9 @@ def main():
     ap.add_argument("--train-steps", type=int, default=1000, help="proposal record: Adam steps")
     ap.add_argument("--no-proposal", action="store_true", help="leave the learned-proposal record out")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--tile", type=int, default=0, help="descent workload: warp tile width (4, 8, 16, 32)")
+    ap.add_argument("--spread", type=int, default=None, choices=[0, 1],
+                    help="descent workload: child masses per lane (0) or spread over the warp (1)")
     ap.add_argument("--eager", action="store_true", help="time eager steps instead of a CUDA-graph replay")
     args = ap.parse_args()
     if args.workload == "proposal":
