@@ -5,6 +5,7 @@
 // arithmetic follows the reference operation by operation (double where it
 // promotes), so the depth order is identical to the CPU oracle's.
 #pragma once
+#include "uds_blendrem.cuh"
 #include "uds_ewa.cuh"
 
 namespace uds {
@@ -40,14 +41,18 @@ __device__ __forceinline__ void depth_order(int K, const float* dist, int* ord) 
 }
 
 // front-to-back blend (alphacompositing.cuh:58-68): fw[id] = rem * w[id],
-// rem *= (1 - w[id]) in double, in depth order
+// rem *= (1 - w[id]) in double, in depth order; the double update is done on
+// the exact integer product (uds_blendrem.cuh) wherever that gives the same
+// float, so the FP64 pipe only sees the rare inputs off that path
 template <int KMAX>
 __device__ __forceinline__ void blend(int K, const int* ord, const float* w, float* fw) {
     float rem = 1.0f;
     for (int q = 0; q < K; ++q) {
         int id = ord[q];
         fw[id] = fmul(rem, w[id]);
-        rem = (float)dmul((double)rem, dsub(1.0, (double)w[id]));
+        float next;
+        if (!blend_rem(rem, w[id], &next)) next = (float)dmul((double)rem, dsub(1.0, (double)w[id]));
+        rem = next;
     }
 }
 
