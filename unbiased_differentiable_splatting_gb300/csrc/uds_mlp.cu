@@ -392,6 +392,10 @@ struct MlpGradSmem {
     __align__(1024) unsigned char h[3][mlp::kTile * mlp::kHid * 2];
     __align__(1024) unsigned char dz[2][mlp::kTile * mlp::kHid * 2];
     __align__(1024) unsigned char dz4[mlp::kTile * mlp::kOut * 2];
+    // weight-gradient operands: dZ^T padded to 128 rows (rows 64 .. 127 stay
+    // zero) and H^T (or X^T), K = the tile's 128 rows
+    __align__(1024) unsigned char at[mlp::kTile * mlp::kTile * 2];
+    __align__(1024) unsigned char bt[mlp::kHid * mlp::kTile * 2];
     float dz4f[mlp::kTile][2];
     float bias[3 * mlp::kHid + mlp::kOut];
     float dbias[3 * mlp::kHid + mlp::kOut];
@@ -424,6 +428,34 @@ __device__ __forceinline__ void stage_transposed(unsigned char* dst, const float
     }
 }
 
+// Row r of a K-major [128 x K] bf16 tile becomes column r of the K-major
+// [K x 128] tile dst (a transposed operand whose K is the tile's rows).
+__device__ __forceinline__ void transpose_row(unsigned char* dst, const unsigned char* src, int r, int K) {
+    for (int k0 = 0; k0 < K; k0 += 8) {
+        uint4 q = *reinterpret_cast<const uint4*>(src + tc::kmajor_offset(r, k0, K));
+        const unsigned short* e = reinterpret_cast<const unsigned short*>(&q);
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+            *reinterpret_cast<unsigned short*>(dst + tc::kmajor_offset(k0 + i, r, mlp::kTile)) = e[i];
+    }
+}
+
+// TMEM columns [col, col + N) (+)= at (128 x 128) * bt (N x 128)^T: a weight
+// gradient dW = dZ^T H summed over the tile's rows on the tensor cores (rows
+// 64 .. 127 of the accumulator stay zero).  Issued by one thread.
+__device__ __forceinline__ void mma_wgrad(uint32_t taddr, uint32_t col, const unsigned char* at,
+                                          const unsigned char* bt, int N, bool accumulate) {
+    const uint32_t lbo = 128, sbo = (uint32_t)(mlp::kTile / 8) * 128;
+    uint32_t idesc = tc::idesc_bf16(128, N);
+    for (int ks = 0; ks < mlp::kTile / 16; ++ks)
+        tc::mma_bf16(taddr + col, tc::smem_desc(tc::smem_u32(at) + ks * 256, lbo, sbo),
+                     tc::smem_desc(tc::smem_u32(bt) + ks * 256, lbo, sbo), idesc, accumulate || ks > 0);
+}
+
+// TMEM columns of k_mlp_grad: activations / input gradients, then the
+// accumulators of dW4 (2 x 64 used), dW3, dW2 (64 x 64) and dW1 (64 x 16)
+constexpr uint32_t kColAct = 0, kColW4 = 64, kColW3 = 128, kColW2 = 192, kColW1 = 256, kGradCols = 512;
+
 // Each block writes its partial gradients (and loss) to its own slice of
 // part (kParams + 1 floats per block, every slot written by one thread);
 // k_mlp_grad_reduce then sums the slices in block order, so the gradient does
@@ -449,11 +481,13 @@ __global__ void __launch_bounds__(128) k_mlp_grad(int R, const float* __restrict
                                               : i < 3 * kHid ? (oB3 - oB1) + i - 2 * kHid : (oB4 - oB1) + i - 3 * kHid)];
         S.dbias[i] = 0.0f;
     }
-    // dz4 columns 2..15 stay zero
+    // dz4 columns 2..15 stay zero; so do rows 64 .. 127 of the transposed
+    // dZ operand
     for (int i = tid; i < kTile * kOut * 2 / 16; i += 128) reinterpret_cast<uint4*>(S.dz4)[i] = make_uint4(0, 0, 0, 0);
+    for (int i = tid; i < kTile * kTile * 2 / 16; i += 128) reinterpret_cast<uint4*>(S.at)[i] = make_uint4(0, 0, 0, 0);
     if (tid == 0) tc::mbar_init(&S.mbar, 1);
     if (warp == 0) {
-        tc::tmem_alloc(&S.taddr, 64);
+        tc::tmem_alloc(&S.taddr, kGradCols);
         tc::tmem_relinquish();
     }
     tc::fence_before_sync();
@@ -464,16 +498,7 @@ __global__ void __launch_bounds__(128) k_mlp_grad(int R, const float* __restrict
     uint32_t lane_base = taddr + ((uint32_t)(warp * 32) << 16);
     uint32_t phase = 0;
     bool ok = true;
-    // register accumulators of the weight gradients:
-    //  W3, W2: thread t owns output o = t / 2, inputs (t % 2) * 32 .. +32
-    //  W1: output o = t / 2, inputs (t % 2) * 8 .. +8
-    //  W4: output row t / 64 (0 or 1), input t % 64
-    float g3[32], g2[32], g1[8], g4 = 0.0f;
-#pragma unroll
-    for (int i = 0; i < 32; ++i) { g3[i] = 0.0f; g2[i] = 0.0f; }
-#pragma unroll
-    for (int i = 0; i < 8; ++i) g1[i] = 0.0f;
-    const int go = tid >> 1, gi = (tid & 1) * 32, gi1 = (tid & 1) * 8;
+    bool first = true;  // the first tile starts the weight-gradient accumulators
     float lsum = 0.0f;
     int tiles = (R + kTile - 1) / kTile;
     for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
@@ -535,25 +560,41 @@ __global__ void __launch_bounds__(128) k_mlp_grad(int R, const float* __restrict
             put_bf16(S.dz4, tc::kmajor_offset(tid, 1, kOut), -d0);
         }
         tc::fence_before_sync();
+        __syncthreads();
+        // ---- backward.  Each layer stages its weight-gradient operands (dZ^T
+        // and the layer input transposed), then one thread issues the input-
+        // gradient GEMM dH = dZ W and the weight-gradient GEMM dW += dZ^T H
+        // on the tensor cores, while the CUDA cores sum the bias gradients.
+        // layer 4: dZ4^T is 16 rows (2 nonzero); rows 16 .. 63 are cleared
+        transpose_row(S.at, S.dz4, tid, kOut);
+        for (int i = tid; i < 48 * kTile * 2 / 16; i += 128)
+            reinterpret_cast<uint4*>(S.at + 16 * kTile * 2)[i] = make_uint4(0, 0, 0, 0);
+        transpose_row(S.bt, S.h[2], tid, kHid);
         tc::fence_async_smem();
         __syncthreads();
-        // ---- backward, layer 4: dH3 = dZ4 * W4 (tensor cores), dW4, db4
-        ok = mlp_layer(taddr, S.dz4, S.w4t, kOut, kHid, &S.mbar, phase);
-        if (!ok) break;
-        {
-            int o4 = tid >> 6, i4 = tid & 63;
-            for (int r = 0; r < kTile; ++r)
-                g4 = fmaf(S.dz4f[r][o4], get_bf16(S.h[2], tc::kmajor_offset(r, i4, kHid)), g4);
-            if (tid < 2) {
-                float sb = 0.0f;
-                for (int r = 0; r < kTile; ++r) sb += S.dz4f[r][tid];
-                S.dbias[3 * kHid + tid] += sb;
-            }
+        if (tid == 0) {
+            tc::fence_after_sync();
+            uint32_t idesc = tc::idesc_bf16(128, kHid);
+            for (int ks = 0; ks < kOut / 16; ++ks)
+                tc::mma_bf16(taddr + kColAct, tc::smem_desc(tc::smem_u32(S.dz4) + ks * 256, 128, (kOut / 8) * 128),
+                             tc::smem_desc(tc::smem_u32(S.w4t) + ks * 256, 128, (kOut / 8) * 128), idesc, ks > 0);
+            mma_wgrad(taddr, kColW4, S.at, S.bt, kHid, !first);
+            tc::mma_commit(&S.mbar);
         }
+        if (tid < 2) {
+            float sb = 0.0f;
+            for (int r = 0; r < kTile; ++r) sb += S.dz4f[r][tid];
+            S.dbias[3 * kHid + tid] += sb;
+        }
+        ok = tc::mbar_wait(&S.mbar, phase & 1u, kWaitLimit);
+        ++phase;
+        tc::fence_after_sync();
+        ok = __syncthreads_and(ok) != 0;
+        if (!ok) break;
         // dZ3 = dH3 * relu'(Z3) -> dz[0]
         for (int c0 = 0; c0 < kHid; c0 += 16) {
             float v[16];
-            tc::tmem_ld16(lane_base + (uint32_t)c0, v);
+            tc::tmem_ld16(lane_base + kColAct + (uint32_t)c0, v);
 #pragma unroll
             for (int c = 0; c < 16; ++c) {
                 float hv = get_bf16(S.h[2], tc::kmajor_offset(tid, c0 + c, kHid));
@@ -563,31 +604,24 @@ __global__ void __launch_bounds__(128) k_mlp_grad(int R, const float* __restrict
         tc::fence_before_sync();
         tc::fence_async_smem();
         __syncthreads();
-        // layers 3 and 2: dH_{l-1} = dZ_l * W_l on the tensor cores while the
-        // CUDA cores reduce dW_l = dZ_l^T H_{l-1}
+        // layers 3 and 2
         const unsigned char* wt[2] = {S.w3t, S.w2t};
-        float* gacc[2] = {g3, g2};
+        const uint32_t wcol[2] = {kColW3, kColW2};
         for (int l = 0; l < 2 && ok; ++l) {
             const unsigned char* dzl = S.dz[l];
             const unsigned char* hprev = S.h[1 - l];  // H2 for layer 3, H1 for layer 2
+            transpose_row(S.at, dzl, tid, kHid);
+            transpose_row(S.bt, hprev, tid, kHid);
+            tc::fence_async_smem();
+            __syncthreads();
             if (tid == 0) {
                 tc::fence_after_sync();
                 uint32_t idesc = tc::idesc_bf16(128, kHid);
                 for (int ks = 0; ks < kHid / 16; ++ks)
-                    tc::mma_bf16(taddr, tc::smem_desc(tc::smem_u32(dzl) + ks * 256, 128, 8 * 128),
+                    tc::mma_bf16(taddr + kColAct, tc::smem_desc(tc::smem_u32(dzl) + ks * 256, 128, 8 * 128),
                                  tc::smem_desc(tc::smem_u32(wt[l]) + ks * 256, 128, 8 * 128), idesc, ks > 0);
+                mma_wgrad(taddr, wcol[l], S.at, S.bt, kHid, !first);
                 tc::mma_commit(&S.mbar);
-            }
-            float* gg = gacc[l];
-            for (int r = 0; r < kTile; ++r) {
-                float dzv = get_bf16(dzl, tc::kmajor_offset(r, go, kHid));
-#pragma unroll
-                for (int c8 = 0; c8 < 4; ++c8) {
-                    float hv[8];
-                    get8(hprev, r, gi + 8 * c8, kHid, hv);
-#pragma unroll
-                    for (int q = 0; q < 8; ++q) gg[8 * c8 + q] = fmaf(dzv, hv[q], gg[8 * c8 + q]);
-                }
             }
             if (tid < kHid) {
                 float sb = 0.0f;
@@ -603,7 +637,7 @@ __global__ void __launch_bounds__(128) k_mlp_grad(int R, const float* __restrict
             unsigned char* dzn = S.dz[1 - l];
             for (int c0 = 0; c0 < kHid; c0 += 16) {
                 float v[16];
-                tc::tmem_ld16(lane_base + (uint32_t)c0, v);
+                tc::tmem_ld16(lane_base + kColAct + (uint32_t)c0, v);
 #pragma unroll
                 for (int c = 0; c < 16; ++c) {
                     float hv = get_bf16(hprev, tc::kmajor_offset(tid, c0 + c, kHid));
@@ -615,35 +649,57 @@ __global__ void __launch_bounds__(128) k_mlp_grad(int R, const float* __restrict
             __syncthreads();
         }
         if (!ok) break;
-        // layer 1: dW1 = dZ1^T X, db1 (dZ1 is in dz[0] after two swaps)
+        // layer 1: dW1 += dZ1^T X (dZ1 is in dz[0] after two swaps), db1
         {
             const unsigned char* dz1 = S.dz[0];
-            for (int r = 0; r < kTile; ++r) {
-                float dzv = get_bf16(dz1, tc::kmajor_offset(r, go, kHid));
-                float xv[8];
-                get8(S.x, r, gi1, kIn, xv);
-#pragma unroll
-                for (int q = 0; q < 8; ++q) g1[q] = fmaf(dzv, xv[q], g1[q]);
+            transpose_row(S.at, dz1, tid, kHid);
+            transpose_row(S.bt, S.x, tid, kIn);
+            tc::fence_async_smem();
+            __syncthreads();
+            if (tid == 0) {
+                tc::fence_after_sync();
+                mma_wgrad(taddr, kColW1, S.at, S.bt, kIn, !first);
+                tc::mma_commit(&S.mbar);
             }
             if (tid < kHid) {
                 float sb = 0.0f;
                 for (int r = 0; r < kTile; ++r) sb += get_bf16(dz1, tc::kmajor_offset(r, tid, kHid));
                 S.dbias[tid] += sb;
             }
+            ok = tc::mbar_wait(&S.mbar, phase & 1u, kWaitLimit);
+            ++phase;
+            tc::fence_after_sync();
+            ok = __syncthreads_and(ok) != 0;
         }
-        __syncthreads();
+        first = false;
     }
     if (!ok && (tid & 31) == 0) atomicExch(err, 1);
-    // this block's partial sums: one writer per slot, no atomics
+    // this block's partial sums: one writer per slot, no atomics.  Thread t
+    // reads TMEM lane t: row t of each weight-gradient accumulator (rows
+    // 64 .. 127 are the zero padding)
     float* G = part + (size_t)blockIdx.x * kGradPart;
+    if (ok) {
+        for (int c0 = 0; c0 < kHid; c0 += 16) {
+            float v4[16], v3[16], v2[16];
+            tc::tmem_ld16(lane_base + kColW4 + (uint32_t)c0, v4);
+            tc::tmem_ld16(lane_base + kColW3 + (uint32_t)c0, v3);
+            tc::tmem_ld16(lane_base + kColW2 + (uint32_t)c0, v2);
+            if (tid < kHid) {
 #pragma unroll
-    for (int i = 0; i < 32; ++i) {
-        G[oW3 + go * kHid + gi + i] = g3[i];
-        G[oW2 + go * kHid + gi + i] = g2[i];
+                for (int c = 0; c < 16; ++c) {
+                    G[oW3 + tid * kHid + c0 + c] = v3[c];
+                    G[oW2 + tid * kHid + c0 + c] = v2[c];
+                    if (tid < kLogits) G[oW4 + tid * kHid + c0 + c] = v4[c];
+                }
+            }
+        }
+        float v1[16];
+        tc::tmem_ld16(lane_base + kColW1, v1);
+        if (tid < kHid) {
+#pragma unroll
+            for (int c = 0; c < 16; ++c) G[oW1 + tid * kIn + c] = v1[c];
+        }
     }
-#pragma unroll
-    for (int i = 0; i < 8; ++i) G[oW1 + go * kIn + gi1 + i] = g1[i];
-    G[oW4 + (tid >> 6) * kHid + (tid & 63)] = g4;
     for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
     if ((tid & 31) == 0) S.wloss[warp] = lsum;
     tc::fence_before_sync();
@@ -655,7 +711,7 @@ __global__ void __launch_bounds__(128) k_mlp_grad(int R, const float* __restrict
     }
     if (tid < 2) G[oB4 + tid] = S.dbias[3 * kHid + tid];
     if (tid == 0) G[kParams] = (((S.wloss[0] + S.wloss[1]) + S.wloss[2]) + S.wloss[3]) * scale;
-    if (warp == 0) tc::tmem_dealloc(taddr, 64);
+    if (warp == 0) tc::tmem_dealloc(taddr, kGradCols);
 }
 
 // grad += the blocks' partial gradients summed in block order; loss += the
