@@ -376,10 +376,12 @@ __global__ void __launch_bounds__(128) k_mlp_forward_tiles(int R, const int* __r
 // softmax(logits) and the target (p, 1 - p) over R rows, added to G (fp32,
 // kParams entries; the caller zeroes it) and the loss added to loss[0].
 // Per 128-row tile: the forward pass keeps the three hidden activations in
-// shared memory; the backward pass runs dH = dZ * W on the tensor cores
-// (B operand: W transposed, staged once) and the weight and bias gradients
-// (reductions over the batch rows) on the CUDA cores, accumulated in
-// registers across the CTA's tiles and added to G once at the end.
+// shared memory; the backward pass runs dH = dZ * W (B operand: W
+// transposed, staged once) and the weight gradients dW += dZ^T H (operands
+// written transposed, K = the tile's rows) on the tensor cores, the weight
+// gradients accumulating in TMEM across the CTA's tiles, and the bias
+// gradients on the CUDA cores in shared memory; each CTA writes its partial
+// sums once at the end.
 struct MlpGradSmem {
     __align__(1024) unsigned char w1[mlp::kHid * mlp::kIn * 2];
     __align__(1024) unsigned char w2[mlp::kHid * mlp::kHid * 2];
