@@ -64,3 +64,30 @@ def test_views_sweep_keyed_by_view_sizes(tmp_path, monkeypatch):
     assert autotune.lookup_views("test-device", views[::-1], 300, 8) is None
     assert autotune.lookup("test-device", 64, 48, 300, 8) is None
     autotune.reset()
+
+
+def test_sampler_resolves_cached_configuration(tmp_path, monkeypatch):
+    """sampling._descent / _descent_views take the given values first, then
+    the cached configuration for the shape (or list of views), then the
+    defaults; leaf_size="auto" reads only the sweep with leaf sizes."""
+    from unbiased_differentiable_splatting_gb300.cudaExtensions import sampling
+    monkeypatch.setenv("UDS_AUTOTUNE_CACHE", str(tmp_path / "cache.json"))
+    monkeypatch.setitem(sampling._device_names, None, "test-device")  # CPU tensors: device index None
+    autotune.reset()
+    pts = torch.zeros((1, 700, 3))
+    assert sampling._descent(pts, 64, 48, 8) == (8, 0, 0)  # nothing cached: defaults
+    autotune.record("test-device", 64, 48, 700, 8, {"tile_x": 16, "spread": 1}, {})
+    assert sampling._descent(pts, 64, 48, 8) == (16, 0, 1)
+    assert sampling._descent(pts, 64, 48, 8, tile_x=4) == (4, 0, 1)
+    assert sampling._descent(pts, 64, 48, 8, spread=0) == (16, 0, 0)
+    assert sampling._descent(pts, 64, 48, 8, leaf_size=32) == (16, 32, 1)
+    assert sampling._descent(pts, 64, 48, 8, leaf_size="auto") == (16, 0, 1)  # no leaf sweep cached
+    autotune.record("test-device", 64, 48, 700, 8, {"tile_x": 4, "spread": 0, "leaf_size": 16}, {})
+    assert sampling._descent(pts, 64, 48, 8, leaf_size="auto") == (4, 16, 0)
+    assert sampling._descent(pts, 64, 48, 8) == (16, 0, 1)  # the plain entry is unchanged
+    views = [(64, 48, 50.0), (32, 32, 30.0)]
+    assert sampling._descent_views(views, pts, 8) == (16, 0, 1)  # falls back to the first view's shape
+    autotune.record("test-device", 0, 0, 700, 8, {"tile_x": 32, "spread": 0}, {}, views=views)
+    assert sampling._descent_views(views, pts, 8) == (32, 0, 0)
+    assert sampling._descent_views(views, pts, 8, tile_x=8, spread=1) == (8, 0, 1)
+    autotune.reset()
