@@ -56,3 +56,32 @@ def test_sm103a_code_object():
     """The build targets sm_103a only (checked from the build flags)."""
     from unbiased_differentiable_splatting_gb300 import _build
     assert "arch=compute_103a,code=sm_103a" in " ".join(_build.ARCH)
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """The ctypes mirrors of uds_sample_params and uds_view_desc have the C
+    header's size and field offsets (compiled with the host C compiler)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc")
+    if cc is None:
+        pytest.skip("no host C compiler")
+    from unbiased_differentiable_splatting_gb300._lib import SampleParams, ViewDesc
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    structs = {"uds_sample_params": SampleParams, "uds_view_desc": ViewDesc}
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "uds.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = str(tmp_path / "layout")
+    subprocess.run([cc, "-std=c11", "-I", inc, str(src), "-o", exe], check=True)
+    out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
