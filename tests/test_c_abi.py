@@ -6,6 +6,8 @@ import os
 import re
 import subprocess
 
+import pytest
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
@@ -62,7 +64,6 @@ def test_struct_layouts_match_header(tmp_path):
     """The ctypes mirrors of uds_sample_params and uds_view_desc have the C
     header's size and field offsets (compiled with the host C compiler)."""
     import shutil
-    import subprocess
     cc = shutil.which("gcc")
     if cc is None:
         pytest.skip("no host C compiler")
